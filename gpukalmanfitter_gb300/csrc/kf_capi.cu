@@ -1,0 +1,319 @@
+// kf_capi.cu — fit kernels and the C ABI declared in include/gb300kf.h.
+//
+// kf_fit_batch replaces the reference's per-track KalmanFitter::fit call
+// (Fitter/KalmanFitter.hpp:716-768) and its launch by fitKernelThreadPerTrack
+// (Run/GPU/Kernels.cu:6-45): one thread per track, structure-of-arrays inputs,
+// no allocation, stream-ordered.
+
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+
+#include "kf_device.cuh"
+
+using namespace kfd;
+
+namespace {
+
+thread_local char g_err[512] = "";
+
+int32_t fail(int32_t code, const char *fmt, const char *detail = "") {
+  std::snprintf(g_err, sizeof(g_err), fmt, detail);
+  return code;
+}
+
+int32_t cudaFail(cudaError_t e, const char *where) {
+  std::snprintf(g_err, sizeof(g_err), "%s: %s", where, cudaGetErrorString(e));
+  return KF_ERR_CUDA;
+}
+
+// Warp-synchronous driver: lanes step independently and park at heavy actor
+// work (filter update, smoothing, final transport); when every lane of the
+// warp is parked or done the parked lanes run their events together, so the
+// FP64-heavy Kalman algebra executes without divergence.
+template <int BS>
+__global__ void __launch_bounds__(BS) fitFp64Kernel(const __grid_constant__ Params P) {
+  __shared__ PlaneD sp[KF_MAX_PLANES];
+  for (int k = threadIdx.x; k < P.nSurf; k += BS) sp[k] = P.planes[k];
+  __syncthreads();
+  const int64_t i = (int64_t)blockIdx.x * BS + threadIdx.x;
+  Lane L;
+  initLane(L, P, sp, i);
+  for (;;) {
+    if (!L.parked && L.pc != PC_DONE) advance(L, P, sp);
+    const bool waiting = L.parked || L.pc == PC_DONE;
+    if (__all_sync(0xffffffffu, waiting)) {
+      if (L.parked) runEvent(L, P, sp);
+      if (__all_sync(0xffffffffu, L.pc == PC_DONE)) break;
+    }
+  }
+  if (i < P.n) {
+    P.oStatus[i] = L.status;
+    P.oChi2[i] = L.chi2;
+    P.oNMeas[i] = L.measStates;
+    if (P.oNSteps) P.oNSteps[i] = L.rkSteps;
+    if (P.oNTrials) P.oNTrials[i] = L.rkTrials;
+    if (L.status != KF_TRACK_OK && !L.finished) {
+      for (int e = 0; e < 6; ++e) P.oParams[(size_t)e * P.stride + i] = 0.;
+      for (int e = 0; e < 21; ++e) P.oCov[(size_t)e * P.stride + i] = 0.;
+    }
+  }
+}
+
+size_t wsBytes(int64_t n, int32_t nSurf) {
+  return (size_t)nSurf * kStateStride * (size_t)n * sizeof(double);
+}
+
+int32_t checkCommon(const kf_inputs_t *in, const kf_config_t *cfg, const kf_geometry_t *geo,
+                    const kf_field_t *field) {
+  if (!in || !cfg || !geo || !field) return fail(KF_ERR_INVALID_ARGUMENT, "null argument%s");
+  if (in->n_tracks < 0 || in->stride < in->n_tracks)
+    return fail(KF_ERR_INVALID_ARGUMENT, "bad n_tracks/stride%s");
+  if (in->n_surfaces <= 0 || in->n_surfaces > KF_MAX_PLANES || geo->n_planes < in->n_surfaces)
+    return fail(KF_ERR_INVALID_ARGUMENT, "bad n_surfaces (1..64, <= geometry planes)%s");
+  if (!geo->center || !geo->rotation) return fail(KF_ERR_INVALID_ARGUMENT, "null geometry%s");
+  if (field->kind != KF_FIELD_CONSTANT && field->kind != KF_FIELD_GRID3D)
+    return fail(KF_ERR_INVALID_ARGUMENT, "unknown field kind%s");
+  if (field->kind == KF_FIELD_GRID3D &&
+      (!field->grid || field->nx < 2 || field->ny < 2 || field->nz < 2))
+    return fail(KF_ERR_INVALID_ARGUMENT, "bad field grid%s");
+  if (cfg->precision != KF_PRECISION_FP64)
+    return fail(KF_ERR_UNSUPPORTED, "precision mode not available%s");
+  if (cfg->max_steps < 0 || cfg->max_rk_trials < 0)
+    return fail(KF_ERR_INVALID_ARGUMENT, "negative step limits%s");
+  return KF_SUCCESS;
+}
+
+void fillParams(Params &P, const kf_inputs_t *in, const kf_outputs_t *out, const kf_config_t *cfg,
+                const kf_geometry_t *geo, const kf_field_t *field, void *ws) {
+  std::memset(&P, 0, sizeof(P));
+  P.n = in->n_tracks;
+  P.stride = in->stride;
+  P.wsStride = in->n_tracks;
+  P.nSurf = in->n_surfaces;
+  P.maxSteps = cfg->max_steps;
+  P.maxTrials = cfg->max_rk_trials;
+  P.smoothing = cfg->smoothing;
+  P.faithful = cfg->faithful_jacobian;
+  P.tol = cfg->tolerance;
+  P.cutoff = cfg->step_size_cutoff;
+  P.mass = cfg->mass;
+  P.overstep = cfg->overstep_limit;
+  P.surfTol = cfg->on_surface_tol;
+  P.outlierCut = cfg->outlier_chi2_cut;
+  P.meas = in->meas;
+  P.mask = in->hit_mask;
+  P.nplanes = in->n_planes;
+  P.start = in->start_params;
+  P.scov = in->start_cov;
+  P.perigee = in->perigee;
+  P.oParams = out->params;
+  P.oCov = out->cov;
+  P.oChi2 = out->chi2;
+  P.oSmoothed = out->smoothed;
+  P.oStatus = out->status;
+  P.oNMeas = out->n_meas;
+  P.oNSteps = out->n_steps;
+  P.oNTrials = out->n_trials;
+  P.ws = static_cast<double *>(ws);
+  FieldD &F = P.field;
+  F.kind = field->kind;
+  F.scale = field->scale;
+  for (int a = 0; a < 3; ++a) {
+    F.B[a] = field->value[a] * field->scale;
+    F.mn[a] = field->min[a];
+  }
+  F.n[0] = field->nx;
+  F.n[1] = field->ny;
+  F.n[2] = field->nz;
+  if (field->kind == KF_FIELD_GRID3D) {
+    for (int a = 0; a < 3; ++a) {
+      const int na = (a == 0) ? field->nx : (a == 1) ? field->ny : field->nz;
+      F.invw[a] = (na - 1) / (field->max[a] - field->min[a]);
+    }
+  }
+  F.grid = reinterpret_cast<const float4 *>(field->grid);
+  for (int k = 0; k < in->n_surfaces; ++k) {
+    PlaneD &pl = P.planes[k];
+    for (int r = 0; r < 3; ++r) {
+      pl.c[r] = geo->center[3 * k + r];
+      pl.U[r] = geo->rotation[9 * k + 3 * r + 0];
+      pl.V[r] = geo->rotation[9 * k + 3 * r + 1];
+      pl.T[r] = geo->rotation[9 * k + 3 * r + 2];
+    }
+  }
+}
+
+int32_t launchFit(const Params &P, int blockSize, cudaStream_t s) {
+  (void)blockSize;
+  if (P.n == 0) return KF_SUCCESS;
+  constexpr int bs = 128;
+  const unsigned grid = (unsigned)((P.n + bs - 1) / bs);
+  fitFp64Kernel<bs><<<grid, bs, 0, s>>>(P);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cudaFail(e, "fit kernel launch");
+  return KF_SUCCESS;
+}
+
+} // namespace
+
+extern "C" {
+
+int32_t kf_version(void) { return KF_ABI_VERSION; }
+
+const char *kf_last_error_string(void) { return g_err; }
+
+void kf_config_default(kf_config_t *c) {
+  if (!c) return;
+  std::memset(c, 0, sizeof(*c));
+  c->precision = KF_PRECISION_FP64;
+  c->max_steps = 1000;
+  c->max_rk_trials = 10000;
+  c->smoothing = 1;
+  c->tolerance = 1e-4;
+  c->step_size_cutoff = 0.;
+  c->mass = 105.6583755e-3;
+  c->overstep_limit = 0.01;
+  c->on_surface_tol = 1e-4;
+  c->outlier_chi2_cut = 0.;
+  c->faithful_jacobian = 1;
+  c->kernel = KF_KERNEL_AUTO;
+  c->block_size = 0;
+}
+
+size_t kf_workspace_size(const kf_config_t *cfg, int64_t n_tracks, int32_t n_surfaces) {
+  (void)cfg;
+  if (n_tracks <= 0 || n_surfaces <= 0) return 0;
+  return wsBytes(n_tracks, n_surfaces);
+}
+
+int32_t kf_fit_batch(const kf_inputs_t *in, kf_outputs_t *out, const kf_config_t *cfg,
+                     const kf_geometry_t *geo, const kf_field_t *field, void *workspace,
+                     size_t workspace_bytes, void *stream) {
+  int32_t rc = checkCommon(in, cfg, geo, field);
+  if (rc) return rc;
+  if (!out || !out->params || !out->cov || !out->chi2 || !out->status || !out->n_meas)
+    return fail(KF_ERR_INVALID_ARGUMENT, "missing output array%s");
+  if (in->n_tracks > 0 && (!in->meas || !in->start_params || !in->start_cov || !in->perigee))
+    return fail(KF_ERR_INVALID_ARGUMENT, "missing input array%s");
+  if (workspace_bytes < wsBytes(in->n_tracks, in->n_surfaces) || (!workspace && in->n_tracks > 0))
+    return fail(KF_ERR_WORKSPACE_TOO_SMALL, "workspace smaller than kf_workspace_size()%s");
+  Params P;
+  fillParams(P, in, out, cfg, geo, field, workspace);
+  return launchFit(P, cfg->block_size, static_cast<cudaStream_t>(stream));
+}
+
+// ---- host-buffer convenience ----------------------------------------------
+namespace {
+struct Staging {
+  size_t meas, mask, nplanes, start, scov, perigee;
+  size_t params, cov, chi2, status, nmeas, nsteps, ntrials, smoothed, ws, total;
+};
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+Staging stagingLayout(int64_t n, int32_t S, bool withSmoothed) {
+  Staging L{};
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    size_t at = o;
+    o = align256(o + bytes);
+    return at;
+  };
+  L.meas = take((size_t)S * 5 * n * 8);
+  L.mask = take((size_t)n * 8);
+  L.nplanes = take((size_t)n * 4);
+  L.start = take((size_t)6 * n * 8);
+  L.scov = take((size_t)21 * n * 8);
+  L.perigee = take((size_t)3 * n * 8);
+  L.params = take((size_t)6 * n * 8);
+  L.cov = take((size_t)21 * n * 8);
+  L.chi2 = take((size_t)n * 8);
+  L.status = take((size_t)n * 4);
+  L.nmeas = take((size_t)n * 4);
+  L.nsteps = take((size_t)n * 4);
+  L.ntrials = take((size_t)n * 4);
+  L.smoothed = withSmoothed ? take((size_t)S * 27 * n * 8) : 0;
+  L.ws = take(wsBytes(n, S));
+  L.total = o;
+  return L;
+}
+
+// copy `rows` rows of `n` elements from a host SoA with stride `hs` into a
+// compact device SoA (or back)
+cudaError_t copyRows(void *dst, size_t dpitchElems, const void *src, size_t spitchElems,
+                     size_t elem, size_t n, size_t rows, cudaMemcpyKind kind, cudaStream_t s) {
+  if (!rows || !n) return cudaSuccess;
+  return cudaMemcpy2DAsync(dst, dpitchElems * elem, src, spitchElems * elem, n * elem, rows, kind, s);
+}
+} // namespace
+
+size_t kf_host_staging_size(const kf_config_t *cfg, int64_t n_tracks, int32_t n_surfaces,
+                            int32_t with_smoothed) {
+  (void)cfg;
+  if (n_tracks <= 0 || n_surfaces <= 0) return 0;
+  return stagingLayout(n_tracks, n_surfaces, with_smoothed != 0).total;
+}
+
+int32_t kf_fit_batch_host(const kf_inputs_t *hin, kf_outputs_t *hout, const kf_config_t *cfg,
+                          const kf_geometry_t *geo, const kf_field_t *field, void *dev,
+                          size_t bytes, void *stream) {
+  int32_t rc = checkCommon(hin, cfg, geo, field);
+  if (rc) return rc;
+  if (!hout || !hout->params || !hout->cov || !hout->chi2 || !hout->status || !hout->n_meas)
+    return fail(KF_ERR_INVALID_ARGUMENT, "missing output array%s");
+  const int64_t n = hin->n_tracks;
+  if (n == 0) return KF_SUCCESS;
+  const int32_t S = hin->n_surfaces;
+  const bool sm = hout->smoothed != nullptr;
+  const Staging L = stagingLayout(n, S, sm);
+  if (!dev || bytes < L.total)
+    return fail(KF_ERR_WORKSPACE_TOO_SMALL, "staging smaller than kf_host_staging_size()%s");
+  char *d = static_cast<char *>(dev);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t hs = (size_t)hin->stride;
+  cudaError_t e = cudaSuccess;
+  auto chk = [&](cudaError_t x) {
+    if (e == cudaSuccess) e = x;
+  };
+  chk(copyRows(d + L.meas, n, hin->meas, hs, 8, n, (size_t)S * 5, cudaMemcpyHostToDevice, s));
+  if (hin->hit_mask) chk(cudaMemcpyAsync(d + L.mask, hin->hit_mask, n * 8, cudaMemcpyHostToDevice, s));
+  if (hin->n_planes) chk(cudaMemcpyAsync(d + L.nplanes, hin->n_planes, n * 4, cudaMemcpyHostToDevice, s));
+  chk(copyRows(d + L.start, n, hin->start_params, hs, 8, n, 6, cudaMemcpyHostToDevice, s));
+  chk(copyRows(d + L.scov, n, hin->start_cov, hs, 8, n, 21, cudaMemcpyHostToDevice, s));
+  chk(copyRows(d + L.perigee, n, hin->perigee, hs, 8, n, 3, cudaMemcpyHostToDevice, s));
+  if (e != cudaSuccess) return cudaFail(e, "host-to-device copy");
+  kf_inputs_t din = *hin;
+  din.stride = n;
+  din.meas = reinterpret_cast<const double *>(d + L.meas);
+  din.hit_mask = hin->hit_mask ? reinterpret_cast<const uint64_t *>(d + L.mask) : nullptr;
+  din.n_planes = hin->n_planes ? reinterpret_cast<const int32_t *>(d + L.nplanes) : nullptr;
+  din.start_params = reinterpret_cast<const double *>(d + L.start);
+  din.start_cov = reinterpret_cast<const double *>(d + L.scov);
+  din.perigee = reinterpret_cast<const double *>(d + L.perigee);
+  kf_outputs_t dout;
+  dout.params = reinterpret_cast<double *>(d + L.params);
+  dout.cov = reinterpret_cast<double *>(d + L.cov);
+  dout.chi2 = reinterpret_cast<double *>(d + L.chi2);
+  dout.status = reinterpret_cast<int32_t *>(d + L.status);
+  dout.n_meas = reinterpret_cast<int32_t *>(d + L.nmeas);
+  dout.n_steps = reinterpret_cast<int32_t *>(d + L.nsteps);
+  dout.n_trials = reinterpret_cast<int32_t *>(d + L.ntrials);
+  dout.smoothed = sm ? reinterpret_cast<double *>(d + L.smoothed) : nullptr;
+  rc = kf_fit_batch(&din, &dout, cfg, geo, field, d + L.ws, wsBytes(n, S), stream);
+  if (rc) return rc;
+  const size_t os = (size_t)hin->stride; // host outputs share the input stride
+  chk(copyRows(hout->params, os, dout.params, n, 8, n, 6, cudaMemcpyDeviceToHost, s));
+  chk(copyRows(hout->cov, os, dout.cov, n, 8, n, 21, cudaMemcpyDeviceToHost, s));
+  chk(cudaMemcpyAsync(hout->chi2, dout.chi2, n * 8, cudaMemcpyDeviceToHost, s));
+  chk(cudaMemcpyAsync(hout->status, dout.status, n * 4, cudaMemcpyDeviceToHost, s));
+  chk(cudaMemcpyAsync(hout->n_meas, dout.n_meas, n * 4, cudaMemcpyDeviceToHost, s));
+  if (hout->n_steps) chk(cudaMemcpyAsync(hout->n_steps, dout.n_steps, n * 4, cudaMemcpyDeviceToHost, s));
+  if (hout->n_trials) chk(cudaMemcpyAsync(hout->n_trials, dout.n_trials, n * 4, cudaMemcpyDeviceToHost, s));
+  if (sm) chk(copyRows(hout->smoothed, os, dout.smoothed, n, 8, n, (size_t)S * 27, cudaMemcpyDeviceToHost, s));
+  if (e != cudaSuccess) return cudaFail(e, "device-to-host copy");
+  e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cudaFail(e, "stream synchronize");
+  return KF_SUCCESS;
+}
+
+} // extern "C"

@@ -1,0 +1,1212 @@
+// kf_device.cuh — per-track fitter state machine for sm_103a.
+//
+// One thread owns one track.  The arithmetic restates the reference
+// KalmanFitter hot path (paths relative to the reference project root):
+//   EigenStepper::step              Propagator/EigenStepper.ipp:226-332
+//   transportMatrix                 Propagator/EigenStepper.ipp:50-124
+//   covarianceTransport/boundState  Propagator/detail/CovarianceEngine.hpp:106-371
+//   DirectNavigator status/target   Propagator/DirectNavigator.hpp:158-225
+//   updateSingleSurfaceStatus       Propagator/detail/SteppingHelper.hpp:31-65
+//   ConstrainedStep                 Propagator/ConstrainedStep.hpp:22-108
+//   PathLimitReached/SurfaceReached Propagator/StandardAborters.hpp:24-132
+//   KalmanFitter actor/aborter      Fitter/KalmanFitter.hpp:216-393, 682-694
+//   GainMatrixUpdater               Fitter/GainMatrixUpdater.hpp:34-106
+//   GainMatrixSmoother              Fitter/GainMatrixSmoother.hpp:21-94
+//   Plane/Line surfaces             Surfaces/detail/PlaneSurface.ipp, LineSurface.ipp
+//
+// The dense 8x8 and 6x6 products of the reference are evaluated on their
+// structural non-zeros only: the RK transport Jacobian is
+//   [[I, 0, A, a], [0, 1, 0, b], [0, 0, B, c], [0, 0, 0, 1]]
+// (blocks position, time, direction, q/p) and stays in that form under
+// multiplication, and the bound-to-bound Jacobian has a zero last column
+// except J(5,5) = 1 and a unit row 4.  Skipped terms are exact zeros and ones,
+// so the result is the reference's algebra with a different rounding order.
+#pragma once
+
+#include <cfloat>
+#include <cstdint>
+
+#include "../../include/gb300kf.h"
+
+namespace kfd {
+
+constexpr int kStateStride = 79; // doubles per stored measurement state
+// layout of one stored state (smoother input):
+//   [0,6) predicted params, [6,27) predicted cov (upper),
+//   [27,33) filtered params, [33,54) filtered cov, [54,79) jacobian rows
+//   0..3 cols 0..4 (20) and row 5 cols 0..4 (5)
+
+struct PlaneD {
+  double c[3], U[3], V[3], T[3];
+};
+
+struct FieldD {
+  int kind;
+  int n[3];
+  double B[3]; // constant field, scale applied
+  double scale;
+  double mn[3], invw[3];
+  const float4 *grid;
+};
+
+struct Params {
+  int64_t n, stride, wsStride;
+  int nSurf;
+  int maxSteps, maxTrials, smoothing, faithful;
+  double tol, cutoff, mass, overstep, surfTol, outlierCut;
+  const double *meas;
+  const uint64_t *mask;
+  const int32_t *nplanes;
+  const double *start, *scov, *perigee;
+  double *oParams, *oCov, *oChi2, *oSmoothed;
+  int32_t *oStatus, *oNMeas, *oNSteps, *oNTrials;
+  double *ws;
+  FieldD field;
+  PlaneD planes[KF_MAX_PLANES];
+};
+
+// upper-triangle index of (i, j), i <= j, row-major
+__host__ __device__ constexpr int ut(int i, int j) {
+  return i * 6 - (i * (i - 1)) / 2 + (j - i);
+}
+__device__ __forceinline__ int sidx(int i, int j) { return i <= j ? ut(i, j) : ut(j, i); }
+
+// ---------------------------------------------------------------------------
+// Magnetic field lookup: Test::ConstantBField (Test/Helper.hpp:17-22) or the
+// trilinear map (MagneticField/InterpolatedBFieldMap.hpp:178-181).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void getField(const FieldD &F, const double p[3], double B[3]) {
+  if (F.kind == KF_FIELD_CONSTANT) {
+    B[0] = F.B[0];
+    B[1] = F.B[1];
+    B[2] = F.B[2];
+    return;
+  }
+  int idx[3];
+  double f[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    double g = (p[a] - F.mn[a]) * F.invw[a];
+    int i = (int)floor(g);
+    i = min(max(i, 0), F.n[a] - 2);
+    idx[a] = i;
+    f[a] = g - i;
+  }
+  const size_t nx = F.n[0], nxy = (size_t)F.n[0] * F.n[1];
+  const size_t base = (size_t)idx[2] * nxy + (size_t)idx[1] * nx + idx[0];
+  const float4 v000 = __ldg(F.grid + base), v100 = __ldg(F.grid + base + 1);
+  const float4 v010 = __ldg(F.grid + base + nx), v110 = __ldg(F.grid + base + nx + 1);
+  const float4 v001 = __ldg(F.grid + base + nxy), v101 = __ldg(F.grid + base + nxy + 1);
+  const float4 v011 = __ldg(F.grid + base + nxy + nx), v111 = __ldg(F.grid + base + nxy + nx + 1);
+  const double gx = 1 - f[0], gy = 1 - f[1], gz = 1 - f[2];
+  auto tri = [&](double a000, double a100, double a010, double a110, double a001,
+                 double a101, double a011, double a111) {
+    double c00 = a000 * gx + a100 * f[0];
+    double c10 = a010 * gx + a110 * f[0];
+    double c01 = a001 * gx + a101 * f[0];
+    double c11 = a011 * gx + a111 * f[0];
+    double c0 = c00 * gy + c10 * f[1];
+    double c1 = c01 * gy + c11 * f[1];
+    return (c0 * gz + c1 * f[2]) * F.scale;
+  };
+  B[0] = tri(v000.x, v100.x, v010.x, v110.x, v001.x, v101.x, v011.x, v111.x);
+  B[1] = tri(v000.y, v100.y, v010.y, v110.y, v001.y, v101.y, v011.y, v111.y);
+  B[2] = tri(v000.z, v100.z, v010.z, v110.z, v001.z, v101.z, v011.z, v111.z);
+}
+
+__device__ __forceinline__ void cross3(const double a[3], const double b[3], double r[3]) {
+  r[0] = a[1] * b[2] - a[2] * b[1];
+  r[1] = a[2] * b[0] - a[0] * b[2];
+  r[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+// std::max / std::min argument semantics (NaN handling as in the reference)
+__device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }
+__device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }
+
+enum { kAccuracy = 0, kActor = 1, kAborter = 2, kUser = 3 };
+enum { kMissed = 0, kReachable = 1, kOnSurface = 2 };
+enum { PC_PRE = 0, PC_LOOP = 1, PC_ACT = 2, PC_POST = 3, PC_DONE = 4 };
+
+struct Lane {
+  // ---- stepper state (EigenStepper::State)
+  double pos[3], dir[3];
+  double p, q, t;
+  double pathAcc;
+  double ss[4]; // ConstrainedStep values
+  int ssDir;    // ConstrainedStep direction (+1 / -1)
+  int navDir;
+  double JA[3][3], Ja[3], Jb, JB[3][3], Jc[3]; // transport Jacobian blocks
+  double G03[3][4]; // jacToGlobal rows 0-2, cols 0-3
+  double G46[3][2]; // jacToGlobal rows 4-6, cols 2-3
+  double der[7];    // derivative rows 0..6 (row 7 is always 0)
+  double cov[21];
+  // per-leg constants (functions of p only)
+  double qop, dtds, d37;
+  // ---- navigation / actor
+  int next, current, nSeq; // current: -1 none, >=0 plane, -2 target line
+  uint64_t mask;
+  int nHits, measStates, firstPlane;
+  bool targetReached, navBreak, smoothed, finished, result, tn, parked;
+  int pc, steps, status, rkSteps, rkTrials;
+  double chi2;
+  double perigee[3];
+  int64_t idx;
+};
+
+// ---- ConstrainedStep -------------------------------------------------------
+__device__ __forceinline__ double ssMax(const Lane &L) {
+  double m = -DBL_MAX;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) m = (L.ss[i] > m) ? L.ss[i] : m;
+  return m;
+}
+__device__ __forceinline__ double ssMin(const Lane &L) {
+  double m = DBL_MAX;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) m = (L.ss[i] < m) ? L.ss[i] : m;
+  return m;
+}
+__device__ __forceinline__ double ssValue(const Lane &L) {
+  return L.ssDir == 1 ? ssMin(L) : ssMax(L);
+}
+__device__ __forceinline__ void ssRelease(Lane &L, int t) {
+  L.ss[t] = (L.ssDir == 1) ? ssMax(L) : ssMin(L);
+}
+__device__ __forceinline__ void ssUpdate(Lane &L, double v, int t, bool rel) {
+  if (rel) ssRelease(L, t);
+  const double c = L.ss[t];
+  L.ss[t] = fabs(c) < fabs(v) ? c : v;
+}
+__device__ __forceinline__ void ssInit(Lane &L, double value) {
+  L.ssDir = value > 0. ? 1 : -1;
+  L.ss[0] = DBL_MAX * L.ssDir;
+  L.ss[1] = DBL_MAX * L.ssDir;
+  L.ss[2] = DBL_MAX * L.ssDir;
+  L.ss[3] = value;
+}
+
+// per-leg constants: q/p, dt/ds and the dt/d(q/p) coefficient
+__device__ __forceinline__ void legConstants(Lane &L, double mass) {
+  L.qop = L.q / L.p;
+  L.dtds = hypot(1., mass / L.p);
+  L.d37 = mass * mass * L.q / (L.p * L.dtds);
+}
+
+// ---- Jacobian resets -------------------------------------------------------
+__device__ __forceinline__ void resetTransport(Lane &L) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      L.JA[i][j] = 0.;
+      L.JB[i][j] = (i == j) ? 1. : 0.;
+    }
+    L.Ja[i] = 0.;
+    L.Jc[i] = 0.;
+  }
+  L.Jb = 0.;
+#pragma unroll
+  for (int i = 0; i < 7; ++i) L.der[i] = 0.;
+}
+
+// PlaneSurface::initJacobianToGlobal (PlaneSurface.ipp:122-156)
+__device__ __forceinline__ void planeJacToGlobal(Lane &L, const PlaneD &pl) {
+  const double x = L.dir[0], y = L.dir[1], z = L.dir[2];
+  const double cosT = z, sinT = sqrt(x * x + y * y);
+  const double inv = 1. / sinT;
+  const double cosP = x * inv, sinP = y * inv;
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    L.G03[r][0] = pl.U[r];
+    L.G03[r][1] = pl.V[r];
+    L.G03[r][2] = 0.;
+    L.G03[r][3] = 0.;
+  }
+  L.G46[0][0] = (-sinT) * sinP;
+  L.G46[0][1] = cosT * cosP;
+  L.G46[1][0] = sinT * cosP;
+  L.G46[1][1] = cosT * sinP;
+  L.G46[2][0] = 0.;
+  L.G46[2][1] = (-sinT);
+}
+
+// LineSurface::referenceFrame (LineSurface.ipp:46-61), line axis z
+__device__ __forceinline__ void lineFrame(const double mom[3], double X[3], double Y[3],
+                                          double D[3]) {
+  Y[0] = 0.;
+  Y[1] = 0.;
+  Y[2] = 1.;
+  double c[3];
+  cross3(Y, mom, c);
+  const double n = sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+  X[0] = c[0] / n;
+  X[1] = c[1] / n;
+  X[2] = c[2] / n;
+  cross3(X, Y, D);
+}
+
+// ---------------------------------------------------------------------------
+// EigenStepper::step (EigenStepper.ipp:226-332)
+// ---------------------------------------------------------------------------
+__device__ void rkStep(Lane &L, const Params &P) {
+  double Bf[3], Bm[3], Bl[3], k1[3], k2[3], k3[3], k4[3];
+  double err = 0.;
+  const double qop = L.qop;
+  getField(P.field, L.pos, Bf);
+  {
+    double c[3];
+    cross3(L.dir, Bf, c);
+    k1[0] = qop * c[0];
+    k1[1] = qop * c[1];
+    k1[2] = qop * c[2];
+  }
+  long nTrials = 0;
+  double h = ssValue(L);
+  for (;;) {
+    L.rkTrials++;
+    // tryRungeKuttaStep
+    const double h2 = h * h, half_h = h * 0.5;
+    double pos1[3], tmp[3], c[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) pos1[i] = L.pos[i] + half_h * L.dir[i] + (h2 * 0.125) * k1[i];
+    getField(P.field, pos1, Bm);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) tmp[i] = L.dir[i] + half_h * k1[i];
+    cross3(tmp, Bm, c);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) k2[i] = qop * c[i];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) tmp[i] = L.dir[i] + half_h * k2[i];
+    cross3(tmp, Bm, c);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) k3[i] = qop * c[i];
+    double pos2[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) pos2[i] = L.pos[i] + h * L.dir[i] + (h2 * 0.5) * k3[i];
+    getField(P.field, pos2, Bl);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) tmp[i] = L.dir[i] + h * k3[i];
+    cross3(tmp, Bl, c);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) k4[i] = qop * c[i];
+    const double d0 = k1[0] - k2[0] - k3[0] + k4[0];
+    const double d1 = k1[1] - k2[1] - k3[1] + k4[1];
+    const double d2 = k1[2] - k2[2] - k3[2] + k4[2];
+    err = smax(h2 * (fabs(d0) + fabs(d1) + fabs(d2)), 1e-20);
+    if (err <= P.tol) break;
+    const double scale = smin(smax(0.25, pow(P.tol / fabs(2. * err), 0.25)), 4.);
+    const double hn = h * scale;
+    L.ss[kAccuracy] = hn;
+    L.ssDir = hn > 0. ? 1 : -1;
+    h = ssValue(L);
+    if (h * h < P.cutoff * P.cutoff) return;
+    if (nTrials > P.maxTrials) return;
+    nTrials++;
+  }
+  // propagationTime (EigenStepper.ipp:36-47)
+  L.t += h * L.dtds;
+  L.der[3] = L.dtds;
+  // transportMatrix (EigenStepper.ipp:50-124) on its non-zero blocks, and
+  // jacTransport = D * jacTransport
+  {
+    const double half_h = h * 0.5;
+    double dk1dL[3], dk2dL[3], dk3dL[3], dk4dL[3], tmp[3], c[3], cc[3];
+    cross3(L.dir, Bf, dk1dL);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) tmp[i] = L.dir[i] + half_h * k1[i];
+    cross3(tmp, Bm, c);
+    cross3(dk1dL, Bm, cc);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) dk2dL[i] = c[i] + (qop * half_h) * cc[i];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) tmp[i] = L.dir[i] + half_h * k2[i];
+    cross3(tmp, Bm, c);
+    cross3(dk2dL, Bm, cc);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) dk3dL[i] = c[i] + (qop * half_h) * cc[i];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) tmp[i] = L.dir[i] + h * k3[i];
+    cross3(tmp, Bl, c);
+    cross3(dk3dL, Bl, cc);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) dk4dL[i] = c[i] + (qop * h) * cc[i];
+    // dk1dT = qop * [B]x
+    double T1[3][3];
+    T1[0][0] = 0.;
+    T1[0][1] = qop * Bf[2];
+    T1[0][2] = qop * -Bf[1];
+    T1[1][0] = qop * -Bf[2];
+    T1[1][1] = 0.;
+    T1[1][2] = qop * Bf[0];
+    T1[2][0] = qop * Bf[1];
+    T1[2][1] = qop * -Bf[0];
+    T1[2][2] = 0.;
+    // dk(n+1)dT = qop * colcross(I + hh * dkndT, B)
+    double T2[3][3], T3[3][3], T4[3][3];
+    auto nextT = [&](const double (&Tp)[3][3], double hh, const double Bx[3],
+                     double (&To)[3][3]) {
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        double col[3], r[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) col[i] = ((i == j) ? 1. : 0.) + hh * Tp[i][j];
+        cross3(col, Bx, r);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) To[i][j] = qop * r[i];
+      }
+    };
+    nextT(T1, half_h, Bm, T2);
+    nextT(T2, half_h, Bm, T3);
+    nextT(T3, h, Bl, T4);
+    // D blocks: dFdT (A), dGdT (I + Bd), dFdL (a), dGdL (c), D(3,7)
+    double DA[3][3], DB[3][3], Da[3], Dc[3];
+    const double h6 = h / 6.;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        double v = ((i == j) ? 1. : 0.) + h6 * (T1[i][j] + T2[i][j] + T3[i][j]);
+        DA[i][j] = v * h;
+        DB[i][j] = ((i == j) ? 1. : 0.) + h6 * (T1[i][j] + 2. * (T2[i][j] + T3[i][j]) + T4[i][j]);
+      }
+      Da[i] = (h * h) / 6. * (dk1dL[i] + dk2dL[i] + dk3dL[i]);
+      Dc[i] = h6 * (dk1dL[i] + 2. * (dk2dL[i] + dk3dL[i]) + dk4dL[i]);
+    }
+    const double D37 = h * L.d37;
+    // new J = D * J:
+    //  A' = A + DA*B,  a' = a + DA*c + Da,  b' = b + D37,
+    //  B' = DB*B,      c' = DB*c + Dc
+    double nA[3][3], na[3], nB[3][3], nc[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        nA[i][j] = L.JA[i][j] + DA[i][0] * L.JB[0][j] + DA[i][1] * L.JB[1][j] + DA[i][2] * L.JB[2][j];
+        nB[i][j] = DB[i][0] * L.JB[0][j] + DB[i][1] * L.JB[1][j] + DB[i][2] * L.JB[2][j];
+      }
+      na[i] = L.Ja[i] + DA[i][0] * L.Jc[0] + DA[i][1] * L.Jc[1] + DA[i][2] * L.Jc[2] + Da[i];
+      nc[i] = DB[i][0] * L.Jc[0] + DB[i][1] * L.Jc[1] + DB[i][2] * L.Jc[2] + Dc[i];
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        L.JA[i][j] = nA[i][j];
+        L.JB[i][j] = nB[i][j];
+      }
+      L.Ja[i] = na[i];
+      L.Jc[i] = nc[i];
+    }
+    L.Jb = L.Jb + D37;
+  }
+  // equations of motion
+  const double hh6 = h * h / 6., h6 = h / 6.;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    L.pos[i] = L.pos[i] + (h * L.dir[i] + hh6 * (k1[i] + k2[i] + k3[i]));
+    L.dir[i] = L.dir[i] + h6 * (k1[i] + 2. * (k2[i] + k3[i]) + k4[i]);
+  }
+  {
+    const double n = sqrt(L.dir[0] * L.dir[0] + L.dir[1] * L.dir[1] + L.dir[2] * L.dir[2]);
+    const double inv = 1. / n;
+    L.dir[0] *= inv;
+    L.dir[1] *= inv;
+    L.dir[2] *= inv;
+  }
+  L.der[0] = L.dir[0];
+  L.der[1] = L.dir[1];
+  L.der[2] = L.dir[2];
+  L.der[4] = k4[0];
+  L.der[5] = k4[1];
+  L.der[6] = k4[2];
+  L.pathAcc += h;
+  L.rkSteps++;
+}
+
+// ---------------------------------------------------------------------------
+// Covariance transport to a surface (CovarianceEngine.hpp:269-290 with
+// surfaceDerivative :106-125) on the structural non-zeros.
+//   Pt[r][c]  rows 0-2 of jacToGlobal after jacTransport, cols 0..4
+//   R3[c]     row 3, cols 0..4 (col 5 is 1)
+//   Dd[r][c]  rows 4-6, cols 0..4
+// Row 7 is e4 and column 5 is e3 throughout.
+// ---------------------------------------------------------------------------
+struct Transported {
+  double Pt[3][5], R3[5], Dd[3][5];
+};
+
+__device__ __forceinline__ void applyTransport(const Lane &L, Transported &X) {
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    X.Pt[r][0] = L.G03[r][0];
+    X.Pt[r][1] = L.G03[r][1];
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      X.Pt[r][2 + c] = L.G03[r][2 + c] + L.JA[r][0] * L.G46[0][c] +
+                       L.JA[r][1] * L.G46[1][c] + L.JA[r][2] * L.G46[2][c];
+      X.Dd[r][2 + c] = L.JB[r][0] * L.G46[0][c] + L.JB[r][1] * L.G46[1][c] +
+                       L.JB[r][2] * L.G46[2][c];
+    }
+    X.Pt[r][4] = L.Ja[r];
+    X.Dd[r][0] = 0.;
+    X.Dd[r][1] = 0.;
+    X.Dd[r][4] = L.Jc[r];
+  }
+  X.R3[0] = 0.;
+  X.R3[1] = 0.;
+  X.R3[2] = 0.;
+  X.R3[3] = 0.;
+  X.R3[4] = L.Jb;
+}
+
+// jacToGlobal -= derivative * sVec, then J = jacToLocal * jacToGlobal and
+// cov <- J cov J^T.  axis0/axis1 are the surface's local measurement axes
+// (rows 0 and 1 of jacToLocal); the direction rows follow
+// PlaneSurface.ipp:158-189 / LineSurface.ipp:114-143.
+__device__ __forceinline__ void projectCov(Lane &L, Transported &X, const double sVec[5],
+                                           const double ax0[3], const double ax1[3],
+                                           double Jst[25]) {
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      X.Pt[r][c] -= L.der[r] * sVec[c];
+      X.Dd[r][c] -= L.der[4 + r] * sVec[c];
+    }
+    X.R3[c] -= L.der[3] * sVec[c];
+  }
+  const double x = L.dir[0], y = L.dir[1], z = L.dir[2];
+  const double cosT = z, sinT = sqrt(x * x + y * y);
+  const double invS = 1. / sinT;
+  const double cosP = x * invS, sinP = y * invS;
+  const double j24 = -sinP * invS, j25 = cosP * invS;
+  const double j34 = cosP * cosT, j35 = sinP * cosT, j36 = -sinT;
+  double J[6][6];
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    J[0][c] = ax0[0] * X.Pt[0][c] + ax0[1] * X.Pt[1][c] + ax0[2] * X.Pt[2][c];
+    J[1][c] = ax1[0] * X.Pt[0][c] + ax1[1] * X.Pt[1][c] + ax1[2] * X.Pt[2][c];
+    J[2][c] = j24 * X.Dd[0][c] + j25 * X.Dd[1][c];
+    J[3][c] = j34 * X.Dd[0][c] + j35 * X.Dd[1][c] + j36 * X.Dd[2][c];
+    J[4][c] = (c == 4) ? 1. : 0.;
+    J[5][c] = X.R3[c];
+  }
+#pragma unroll
+  for (int r = 0; r < 6; ++r) J[r][5] = (r == 5) ? 1. : 0.;
+  // M = J C  (rows 0-3 and 5 use k = 0..4 (+5 for row 5), row 4 = C row 4)
+  double M[6][6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      if (i == 4) {
+        M[i][j] = L.cov[sidx(4, j)];
+      } else {
+        double s = J[i][0] * L.cov[sidx(0, j)];
+#pragma unroll
+        for (int k = 1; k < 5; ++k) s += J[i][k] * L.cov[sidx(k, j)];
+        if (i == 5) s += L.cov[sidx(5, j)];
+        M[i][j] = s;
+      }
+    }
+  }
+  // C' = M J^T (upper triangle)
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+#pragma unroll
+    for (int j = i; j < 6; ++j) {
+      double s;
+      if (j == 4) {
+        s = M[i][4];
+      } else {
+        s = M[i][0] * J[j][0];
+#pragma unroll
+        for (int k = 1; k < 5; ++k) s += M[i][k] * J[j][k];
+        if (j == 5) s += M[i][5];
+      }
+      L.cov[ut(i, j)] = s;
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    Jst[c] = J[0][c];
+    Jst[5 + c] = J[1][c];
+    Jst[10 + c] = J[2][c];
+    Jst[15 + c] = J[3][c];
+    Jst[20 + c] = J[5][c];
+  }
+}
+
+// BoundParameters from the free state (CovarianceEngine.hpp:363-370 and
+// coordinate_transformations.hpp:115-128): angles and q/p from the momentum.
+__device__ __forceinline__ void boundAngles(const Lane &L, double out[6], double mom[3]) {
+  const double qopF = L.q / L.p;
+  const double pabs = fabs(1. / qopF);
+  mom[0] = pabs * L.dir[0];
+  mom[1] = pabs * L.dir[1];
+  mom[2] = pabs * L.dir[2];
+  const double charge = copysign(1., qopF);
+  const double pt = sqrt(mom[0] * mom[0] + mom[1] * mom[1]);
+  out[2] = atan2(mom[1], mom[0]);
+  out[3] = atan2(pt, mom[2]);
+  out[4] = ((fabs(charge) < 1e-4) ? 1. : charge) /
+           sqrt(mom[0] * mom[0] + mom[1] * mom[1] + mom[2] * mom[2]);
+  out[5] = L.t;
+}
+
+// boundState<PlaneSurface> (EigenStepper.ipp:516-540) incl. re-initialisation
+__device__ void boundStatePlane(Lane &L, const PlaneD &pl, double out[6], double Jst[25]) {
+  Transported X;
+  applyTransport(L, X);
+  // PlaneSurface::derivativeFactors (PlaneSurface.ipp:191-204)
+  const double dp = pl.T[0] * L.dir[0] + pl.T[1] * L.dir[1] + pl.T[2] * L.dir[2];
+  const double nv0 = pl.T[0] / dp, nv1 = pl.T[1] / dp, nv2 = pl.T[2] / dp;
+  double sVec[5];
+#pragma unroll
+  for (int c = 0; c < 5; ++c) sVec[c] = nv0 * X.Pt[0][c] + nv1 * X.Pt[1][c] + nv2 * X.Pt[2][c];
+  projectCov(L, X, sVec, pl.U, pl.V, Jst);
+  // reinitializeJacobians (CovarianceEngine.hpp:169-201)
+  resetTransport(L);
+  planeJacToGlobal(L, pl);
+  const double d0 = L.pos[0] - pl.c[0], d1 = L.pos[1] - pl.c[1], d2 = L.pos[2] - pl.c[2];
+  out[0] = pl.U[0] * d0 + pl.U[1] * d1 + pl.U[2] * d2;
+  out[1] = pl.V[0] * d0 + pl.V[1] * d1 + pl.V[2] * d2;
+  double mom[3];
+  boundAngles(L, out, mom);
+}
+
+// boundState<LineSurface> towards the perigee line (axis z through `c`)
+__device__ void boundStateLine(Lane &L, const double c[3], double out[6]) {
+  Transported X;
+  applyTransport(L, X);
+  double mX[3], mY[3], mD[3];
+  lineFrame(L.dir, mX, mY, mD);
+  // LineSurface::derivativeFactors (LineSurface.ipp:145-182), locz = (0,0,1)
+  const double pc0 = L.pos[0] - c[0], pc1 = L.pos[1] - c[1], pc2 = L.pos[2] - c[2];
+  const double long_c = mY[0] * L.dir[0] + mY[1] * L.dir[1] + mY[2] * L.dir[2];
+  const double nv0 = L.dir[0] - long_c * mY[0], nv1 = L.dir[1] - long_c * mY[1],
+               nv2 = L.dir[2] - long_c * mY[2];
+  const double nrm = 1. / (1. - long_c * long_c);
+  double sVec[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const double s = nv0 * X.Pt[0][k] + nv1 * X.Pt[1][k] + nv2 * X.Pt[2][k];
+    const double e0 = mY[0] * s - X.Dd[0][k], e1 = mY[1] * s - X.Dd[1][k],
+                 e2 = mY[2] * s - X.Dd[2][k];
+    const double row = pc0 * e0 + pc1 * e1 + pc2 * e2;
+    sVec[k] = nrm * (s - row);
+  }
+  double Jst[25];
+  projectCov(L, X, sVec, mX, mY, Jst);
+  double mom[3];
+  boundAngles(L, out, mom);
+  // LineSurface::globalToLocal (LineSurface.ipp:200-220)
+  const double r = sqrt(pc0 * pc0 + pc1 * pc1);
+  // (z x mom) . (pos - c)
+  const double sgn = ((-mom[1]) * pc0 + mom[0] * pc1 < 0.) ? -1. : 1.;
+  out[0] = r * sgn;
+  out[1] = pc2;
+}
+
+// EigenStepper::update (EigenStepper.ipp:554-564) from bound parameters on a
+// plane (boundParameters2freeParameters, coordinate_transformations.hpp:145-158)
+__device__ __forceinline__ void stepperUpdate(Lane &L, const PlaneD &pl, const double par[6],
+                                              const double cov[21], double mass) {
+#pragma unroll
+  for (int r = 0; r < 3; ++r) L.pos[r] = pl.U[r] * par[0] + pl.V[r] * par[1] + pl.c[r];
+  double sp, cp, st, ct;
+  sincos(par[2], &sp, &cp);
+  sincos(par[3], &st, &ct);
+  const double d0 = cp * st, d1 = sp * st, d2 = ct;
+  const double n = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+  L.dir[0] = d0 / n;
+  L.dir[1] = d1 / n;
+  L.dir[2] = d2 / n;
+  L.p = fabs(1. / par[4]);
+  L.t = par[5];
+#pragma unroll
+  for (int e = 0; e < 21; ++e) L.cov[e] = cov[e];
+  legConstants(L, mass);
+}
+
+// ---------------------------------------------------------------------------
+// Workspace access: state s of track i, element e
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double *wsPtr(const Params &P, const Lane &L, int s, int e) {
+  return P.ws + ((size_t)s * kStateStride + e) * (size_t)P.wsStride + L.idx;
+}
+
+// ---------------------------------------------------------------------------
+// Actor::filter (KalmanFitter.hpp:284-350) for a plane that has a hit, with
+// GainMatrixUpdater (GainMatrixUpdater.hpp:34-106)
+// ---------------------------------------------------------------------------
+__device__ void filterHit(Lane &L, const Params &P, const PlaneD *planes, int k) {
+  const PlaneD &pl = planes[k];
+  double pred[6], Jst[25];
+  boundStatePlane(L, pl, pred, Jst);
+  const double *mp = P.meas + (size_t)k * 5 * P.stride + L.idx;
+  const double m0 = mp[0], m1 = mp[P.stride], v00 = mp[2 * P.stride],
+               v01 = mp[3 * P.stride], v11 = mp[4 * P.stride];
+  const double S00 = L.cov[0] + v00, S01 = L.cov[1] + v01, S10 = L.cov[1] + v01,
+               S11 = L.cov[6] + v11;
+  const double det = S00 * S11 - S01 * S10;
+  const double i00 = S11 / det, i01 = -S01 / det, i10 = -S10 / det, i11 = S00 / det;
+  const double r0 = m0 - pred[0], r1 = m1 - pred[1];
+  const double chi2 = r0 * (i00 * r0 + i01 * r1) + r1 * (i10 * r0 + i11 * r1);
+  const bool outlier = (P.outlierCut > 0. && chi2 > P.outlierCut);
+  const int s = L.measStates;
+  if (s == 0) L.firstPlane = k;
+  // store predicted state and Jacobian
+#pragma unroll
+  for (int e = 0; e < 6; ++e) *wsPtr(P, L, s, e) = pred[e];
+#pragma unroll
+  for (int e = 0; e < 21; ++e) *wsPtr(P, L, s, 6 + e) = L.cov[e];
+#pragma unroll
+  for (int e = 0; e < 25; ++e) *wsPtr(P, L, s, 54 + e) = Jst[e];
+  if (outlier) {
+#pragma unroll
+    for (int e = 0; e < 6; ++e) *wsPtr(P, L, s, 27 + e) = pred[e];
+#pragma unroll
+    for (int e = 0; e < 21; ++e) *wsPtr(P, L, s, 33 + e) = L.cov[e];
+  } else {
+    double K0[6], K1[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      const double c0 = L.cov[sidx(i, 0)], c1 = L.cov[sidx(i, 1)];
+      K0[i] = c0 * i00 + c1 * i10;
+      K1[i] = c0 * i01 + c1 * i11;
+    }
+    double filt[6], cf[21];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) filt[i] = pred[i] + (K0[i] * r0 + K1[i] * r1);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+#pragma unroll
+      for (int j = i; j < 6; ++j)
+        cf[ut(i, j)] = L.cov[ut(i, j)] - K0[i] * L.cov[sidx(0, j)] - K1[i] * L.cov[sidx(1, j)];
+    }
+#pragma unroll
+    for (int e = 0; e < 6; ++e) *wsPtr(P, L, s, 27 + e) = filt[e];
+#pragma unroll
+    for (int e = 0; e < 21; ++e) *wsPtr(P, L, s, 33 + e) = cf[e];
+    L.chi2 += chi2;
+    stepperUpdate(L, pl, filt, cf, P.mass);
+    if (!P.faithful) planeJacToGlobal(L, pl);
+  }
+  L.measStates++;
+}
+
+// Symmetric 6x6 inverse by LDL^T (the predicted covariance is positive
+// definite); input and output upper triangles.
+__device__ __forceinline__ void invSym6(const double A[21], double Inv[21]) {
+  double Lm[6][6], d[6], rd[6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    double v = A[ut(j, j)];
+#pragma unroll
+    for (int k = 0; k < j; ++k) v -= Lm[j][k] * Lm[j][k] * d[k];
+    d[j] = v;
+    rd[j] = 1. / v;
+#pragma unroll
+    for (int i = j + 1; i < 6; ++i) {
+      double w = A[ut(j, i)];
+#pragma unroll
+      for (int k = 0; k < j; ++k) w -= Lm[i][k] * Lm[j][k] * d[k];
+      Lm[i][j] = w * rd[j];
+    }
+  }
+  // Y = L^-1 (unit lower)
+  double Y[6][6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+#pragma unroll
+    for (int j = 0; j < i; ++j) {
+      double v = -Lm[i][j];
+#pragma unroll
+      for (int k = j + 1; k < i; ++k) v -= Lm[i][k] * Y[k][j];
+      Y[i][j] = v;
+    }
+  }
+  // Inv = Y^T D^-1 Y
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+#pragma unroll
+    for (int j = i; j < 6; ++j) {
+      double v = rd[j] * ((j == i) ? 1. : Y[j][i]);
+#pragma unroll
+      for (int k = j + 1; k < 6; ++k) v += Y[k][i] * rd[k] * Y[k][j];
+      Inv[ut(i, j)] = v;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Actor::finalize (KalmanFitter.hpp:360-393) with GainMatrixSmoother
+// (GainMatrixSmoother.hpp:21-94).  Returns false on a NaN gain.
+// ---------------------------------------------------------------------------
+__device__ bool finalizeSmooth(Lane &L, const Params &P, const PlaneD *planes) {
+  L.smoothed = true;
+  const int n = L.measStates;
+  double xs[6], Cs[21];
+#pragma unroll
+  for (int e = 0; e < 6; ++e) xs[e] = *wsPtr(P, L, n - 1, 27 + e);
+#pragma unroll
+  for (int e = 0; e < 21; ++e) Cs[e] = *wsPtr(P, L, n - 1, 33 + e);
+  if (P.oSmoothed) {
+#pragma unroll
+    for (int e = 0; e < 6; ++e)
+      P.oSmoothed[((size_t)(n - 1) * 27 + e) * P.stride + L.idx] = xs[e];
+#pragma unroll
+    for (int e = 0; e < 21; ++e)
+      P.oSmoothed[((size_t)(n - 1) * 27 + 6 + e) * P.stride + L.idx] = Cs[e];
+  }
+  for (int i = n - 2; i >= 0; --i) {
+    double xp[6], Cp[21], Jn[25], xf[6], Cf[21];
+#pragma unroll
+    for (int e = 0; e < 6; ++e) xp[e] = *wsPtr(P, L, i + 1, e);
+#pragma unroll
+    for (int e = 0; e < 21; ++e) Cp[e] = *wsPtr(P, L, i + 1, 6 + e);
+#pragma unroll
+    for (int e = 0; e < 25; ++e) Jn[e] = *wsPtr(P, L, i + 1, 54 + e);
+#pragma unroll
+    for (int e = 0; e < 6; ++e) xf[e] = *wsPtr(P, L, i, 27 + e);
+#pragma unroll
+    for (int e = 0; e < 21; ++e) Cf[e] = *wsPtr(P, L, i, 33 + e);
+    double inv[21];
+    invSym6(Cp, inv);
+    // A = Cf J^T (J rows 0-3,5 have cols 0..4; row 4 = e4; col 5 = e5 on row 5)
+    double A[6][6];
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        if (c == 4) {
+          A[r][c] = Cf[sidx(r, 4)];
+        } else {
+          const int jr = (c == 5) ? 4 : c; // row of the stored Jacobian
+          double s = Cf[sidx(r, 0)] * Jn[5 * jr + 0];
+#pragma unroll
+          for (int k = 1; k < 5; ++k) s += Cf[sidx(r, k)] * Jn[5 * jr + k];
+          if (c == 5) s += Cf[sidx(r, 5)];
+          A[r][c] = s;
+        }
+      }
+    }
+    // G = A inv
+    double G[6][6];
+    bool nan = false;
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        double s = A[r][0] * inv[sidx(0, c)];
+#pragma unroll
+        for (int k = 1; k < 6; ++k) s += A[r][k] * inv[sidx(k, c)];
+        G[r][c] = s;
+        nan = nan || (s != s);
+      }
+    }
+    if (nan) return false;
+    double dx[6], D[21];
+#pragma unroll
+    for (int e = 0; e < 6; ++e) dx[e] = xs[e] - xp[e];
+#pragma unroll
+    for (int e = 0; e < 21; ++e) D[e] = Cp[e] - Cs[e];
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+      double g = G[r][0] * dx[0];
+#pragma unroll
+      for (int k = 1; k < 6; ++k) g += G[r][k] * dx[k];
+      xs[r] = xf[r] + g;
+    }
+    double W[6][6];
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        double s = G[r][0] * D[sidx(0, c)];
+#pragma unroll
+        for (int k = 1; k < 6; ++k) s += G[r][k] * D[sidx(k, c)];
+        W[r][c] = s;
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+#pragma unroll
+      for (int c = r; c < 6; ++c) {
+        double s = W[r][0] * G[c][0];
+#pragma unroll
+        for (int k = 1; k < 6; ++k) s += W[r][k] * G[c][k];
+        Cs[ut(r, c)] = Cf[ut(r, c)] - s;
+      }
+    }
+    if (P.oSmoothed) {
+#pragma unroll
+      for (int e = 0; e < 6; ++e)
+        P.oSmoothed[((size_t)i * 27 + e) * P.stride + L.idx] = xs[e];
+#pragma unroll
+      for (int e = 0; e < 21; ++e)
+        P.oSmoothed[((size_t)i * 27 + 6 + e) * P.stride + L.idx] = Cs[e];
+    }
+  }
+  const PlaneD &pl = planes[L.firstPlane];
+  stepperUpdate(L, pl, xs, Cs, P.mass);
+  if (!P.faithful) planeJacToGlobal(L, pl);
+  L.navDir = -1;
+  ssInit(L, -1. * DBL_MAX);
+  L.pathAcc = 0.;
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Navigation (DirectNavigator.hpp:158-225, SteppingHelper.hpp:31-65)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int updateSurfaceStatus(Lane &L, const Params &P, const PlaneD &pl) {
+  const double d0 = L.navDir * L.dir[0], d1 = L.navDir * L.dir[1], d2 = L.navDir * L.dir[2];
+  const double denom = d0 * pl.T[0] + d1 * pl.T[1] + d2 * pl.T[2];
+  if (denom != 0.0) {
+    const double path = (pl.T[0] * (pl.c[0] - L.pos[0]) + pl.T[1] * (pl.c[1] - L.pos[1]) +
+                         pl.T[2] * (pl.c[2] - L.pos[2])) /
+                        denom;
+    if (path * path < P.surfTol * P.surfTol) {
+      ssRelease(L, kActor);
+      return kOnSurface;
+    }
+    const double pLimit = L.ss[kAborter];
+    const double oLimit = -P.overstep;
+    if (path > oLimit && path * path < pLimit * pLimit) {
+      ssUpdate(L, L.navDir * path, kActor, true);
+      return kReachable;
+    }
+  }
+  return kMissed;
+}
+
+__device__ __forceinline__ void navStatus(Lane &L, const Params &P, const PlaneD *planes) {
+  L.current = -1;
+  if (L.next != L.nSeq) {
+    if (updateSurfaceStatus(L, P, planes[L.next]) == kOnSurface) {
+      L.current = L.next;
+      ++L.next;
+      if (L.next != L.nSeq) ssRelease(L, kActor);
+    }
+  }
+}
+
+__device__ __forceinline__ void navTarget(Lane &L, const Params &P, const PlaneD *planes) {
+  L.current = -1;
+  if (L.next != L.nSeq) {
+    if (updateSurfaceStatus(L, P, planes[L.next]) == kMissed) ++L.next;
+  } else {
+    L.navBreak = true;
+  }
+}
+
+// LineSurface::intersect (LineSurface.ipp:229-262) along navDir * dir
+__device__ __forceinline__ void lineIntersect(const Lane &L, const Params &P, double &u,
+                                              int &status) {
+  const double ea0 = L.navDir * L.dir[0], ea1 = L.navDir * L.dir[1], ea2 = L.navDir * L.dir[2];
+  const double m0 = L.perigee[0] - L.pos[0], m1 = L.perigee[1] - L.pos[1],
+               m2 = L.perigee[2] - L.pos[2];
+  const double eaTeb = ea2;
+  const double denom = 1 - eaTeb * eaTeb;
+  if (denom * denom > P.surfTol * P.surfTol) {
+    u = ((m0 * ea0 + m1 * ea1 + m2 * ea2) - m2 * eaTeb) / denom;
+    status = (u * u < P.surfTol * P.surfTol) ? kOnSurface : kReachable;
+  } else {
+    u = DBL_MAX;
+    status = kMissed;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// The Kalman actor (KalmanFitter.hpp:216-273).  With heavy == false it only
+// runs when no filter update, smoothing or final transport is due, and
+// returns false without touching the state otherwise.
+// ---------------------------------------------------------------------------
+__device__ bool actor(Lane &L, const Params &P, const PlaneD *planes, bool heavy) {
+  const bool onPlane = L.current >= 0 && !L.smoothed && !L.finished;
+  const bool hit = onPlane && ((L.mask >> L.current) & 1ull);
+  if (!heavy) {
+    const int ms = L.measStates + (hit ? 1 : 0);
+    const bool fin = (ms == L.nHits || (ms > 0 && L.navBreak)) && !L.smoothed && !L.finished &&
+                     P.smoothing;
+    if (hit || fin) return false;
+    if (L.smoothed && !L.finished) {
+      if (L.targetReached || L.current == -2) return false;
+      double u;
+      int st;
+      lineIntersect(L, P, u, st);
+      if (st == kOnSurface) return false;
+    }
+  }
+  if (hit) filterHit(L, P, planes, L.current);
+  if ((L.measStates == L.nHits || (L.measStates > 0 && L.navBreak)) && !L.smoothed &&
+      !L.finished) {
+    if (!P.smoothing) {
+      L.finished = true;
+    } else if (!finalizeSmooth(L, P, planes)) {
+      L.result = false;
+    }
+  }
+  if (L.smoothed && !L.finished) {
+    // SurfaceReached (StandardAborters.hpp:88-132)
+    bool reached;
+    if (L.targetReached) {
+      reached = true;
+    } else if (L.current == -2) {
+      L.targetReached = true;
+      reached = true;
+    } else {
+      double u;
+      int st;
+      lineIntersect(L, P, u, st);
+      reached = (st == kOnSurface);
+      if (reached) {
+        L.current = -2;
+        L.targetReached = true;
+      } else {
+        ssUpdate(L, L.navDir * u, kAborter, false);
+      }
+    }
+    if (reached) {
+      double out[6];
+      boundStateLine(L, L.perigee, out);
+#pragma unroll
+      for (int e = 0; e < 6; ++e) P.oParams[(size_t)e * P.stride + L.idx] = out[e];
+#pragma unroll
+      for (int e = 0; e < 21; ++e) P.oCov[(size_t)e * P.stride + L.idx] = L.cov[e];
+      L.finished = true;
+    }
+  }
+  return true;
+}
+
+// Kalman aborter (KalmanFitter.hpp:682-694) then PathLimitReached
+// (StandardAborters.hpp:37-56)
+__device__ __forceinline__ bool aborters(Lane &L, const Params &P) {
+  if (!L.result || L.finished) return true;
+  if (L.targetReached) return true;
+  const double distance = L.navDir * fabs(DBL_MAX) - L.pathAcc;
+  ssUpdate(L, distance, kAborter, false);
+  const bool limit = distance * distance < P.surfTol * P.surfTol;
+  if (limit) L.targetReached = true;
+  return limit;
+}
+
+__device__ __forceinline__ void finish(Lane &L, const Params &P) {
+  int st;
+  if (!L.result)
+    st = L.smoothed ? KF_TRACK_SMOOTHER_NAN : KF_TRACK_MEAS_MISMATCH;
+  else if (L.measStates != L.nHits)
+    st = KF_TRACK_MEAS_MISMATCH;
+  else if (!L.tn)
+    st = KF_TRACK_MAX_STEPS;
+  else if (P.smoothing && !L.finished)
+    st = KF_TRACK_NOT_FITTED;
+  else
+    st = KF_TRACK_OK;
+  L.status = st;
+}
+
+// ---------------------------------------------------------------------------
+// Propagator::propagate (Propagator.ipp:6-96) as a resumable program:
+// advance() runs cheap iterations until the next RK step is done, an event
+// (heavy actor work) is due, or the track is done; runEvent() executes the
+// pending actor call with heavy work allowed and continues.
+// ---------------------------------------------------------------------------
+__device__ void advance(Lane &L, const Params &P, const PlaneD *planes) {
+  for (;;) {
+    switch (L.pc) {
+    case PC_PRE:
+      if (!actor(L, P, planes, false)) {
+        L.parked = true;
+        return;
+      }
+      if (aborters(L, P)) {
+        L.pc = PC_POST;
+      } else {
+        navTarget(L, P, planes);
+        L.pc = PC_LOOP;
+      }
+      continue;
+    case PC_LOOP:
+      if (L.steps >= P.maxSteps) {
+        L.pc = PC_POST;
+        continue;
+      }
+      rkStep(L, P);
+      navStatus(L, P, planes);
+      L.pc = PC_ACT;
+      continue;
+    case PC_ACT:
+      if (!actor(L, P, planes, false)) {
+        L.parked = true;
+        return;
+      }
+      if (aborters(L, P)) {
+        L.tn = true;
+        L.pc = PC_POST;
+        continue;
+      }
+      navTarget(L, P, planes);
+      L.steps++;
+      L.pc = PC_LOOP;
+      return;
+    case PC_POST:
+      if (!L.tn) L.navBreak = true;
+      if (!actor(L, P, planes, false)) {
+        L.parked = true;
+        return;
+      }
+      finish(L, P);
+      L.pc = PC_DONE;
+      return;
+    default:
+      return;
+    }
+  }
+}
+
+__device__ void runEvent(Lane &L, const Params &P, const PlaneD *planes) {
+  L.parked = false;
+  switch (L.pc) {
+  case PC_PRE:
+    actor(L, P, planes, true);
+    if (aborters(L, P)) {
+      L.pc = PC_POST;
+    } else {
+      navTarget(L, P, planes);
+      L.pc = PC_LOOP;
+    }
+    break;
+  case PC_ACT:
+    actor(L, P, planes, true);
+    if (aborters(L, P)) {
+      L.tn = true;
+      L.pc = PC_POST;
+    } else {
+      navTarget(L, P, planes);
+      L.steps++;
+      L.pc = PC_LOOP;
+    }
+    break;
+  case PC_POST:
+    actor(L, P, planes, true);
+    finish(L, P);
+    L.pc = PC_DONE;
+    break;
+  default:
+    break;
+  }
+}
+
+// EigenStepper::State from BoundParameters<LineSurface> (EigenStepper.hpp:40-61)
+// and the navigator initialisation; returns false for unusable input.
+__device__ void initLane(Lane &L, const Params &P, const PlaneD *planes, int64_t i) {
+  L.idx = i;
+  L.pc = PC_DONE;
+  L.parked = false;
+  L.steps = 0;
+  L.rkSteps = 0;
+  L.rkTrials = 0;
+  L.chi2 = 0.;
+  L.measStates = 0;
+  L.firstPlane = 0;
+  L.next = 0;
+  L.current = -1;
+  L.targetReached = false;
+  L.navBreak = false;
+  L.smoothed = false;
+  L.finished = false;
+  L.result = true;
+  L.tn = false;
+  L.status = KF_TRACK_NOT_FITTED;
+  if (i >= P.n) return;
+  double sp[6];
+#pragma unroll
+  for (int e = 0; e < 6; ++e) sp[e] = P.start[(size_t)e * P.stride + i];
+#pragma unroll
+  for (int e = 0; e < 3; ++e) L.perigee[e] = P.perigee[(size_t)e * P.stride + i];
+  int ns = P.nplanes ? P.nplanes[i] : P.nSurf;
+  L.nSeq = min(max(ns, 0), P.nSurf);
+  L.mask = P.mask ? P.mask[i] : ~0ull;
+  L.nHits = __popcll(L.mask & ((L.nSeq >= 64) ? ~0ull : ((1ull << L.nSeq) - 1ull)));
+  bool ok = isfinite(sp[4]) && sp[4] != 0.;
+#pragma unroll
+  for (int e = 0; e < 6; ++e) ok = ok && isfinite(sp[e]);
+  if (!ok) {
+    L.status = KF_TRACK_BAD_INPUT;
+    return;
+  }
+  if (L.nHits == 0) {
+    L.status = KF_TRACK_NO_HITS;
+    return;
+  }
+  // momentum and position on the line (coordinate_transformations.hpp:45-76,
+  // LineSurface.ipp:184-198)
+  const double pabs = fabs(1. / sp[4]);
+  double sph, cph, sth, cth;
+  sincos(sp[2], &sph, &cph);
+  sincos(sp[3], &sth, &cth);
+  const double mom[3] = {pabs * sth * cph, pabs * sth * sph, pabs * cth};
+  const double rad0 = -mom[1], rad1 = mom[0]; // (0,0,1) x mom
+  const double rn = sqrt(rad0 * rad0 + rad1 * rad1);
+  L.pos[0] = L.perigee[0] + sp[0] * (rad0 / rn);
+  L.pos[1] = L.perigee[1] + sp[0] * (rad1 / rn);
+  L.pos[2] = (sp[1] + L.perigee[2]) + sp[0] * (0. / rn);
+  const double pn = sqrt(mom[0] * mom[0] + mom[1] * mom[1] + mom[2] * mom[2]);
+  L.dir[0] = mom[0] / pn;
+  L.dir[1] = mom[1] / pn;
+  L.dir[2] = mom[2] / pn;
+  L.p = pn;
+  L.q = (sp[4] > 0) ? 1. : -1.;
+  L.t = sp[5];
+  L.navDir = 1;
+  ssInit(L, DBL_MAX);
+  L.pathAcc = 0.;
+  resetTransport(L);
+#pragma unroll
+  for (int e = 0; e < 21; ++e) L.cov[e] = P.scov[(size_t)e * P.stride + i];
+  legConstants(L, P.mass);
+  // LineSurface::initJacobianToGlobal (LineSurface.ipp:63-112)
+  {
+    const double x = L.dir[0], y = L.dir[1], z = L.dir[2];
+    const double cosT = z, sinT = sqrt(x * x + y * y);
+    const double inv = 1. / sinT;
+    const double cosP = x * inv, sinP = y * inv;
+    double X[3], Y[3], D[3];
+    lineFrame(L.dir, X, Y, D);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      L.G03[r][0] = X[r];
+      L.G03[r][1] = Y[r];
+    }
+    L.G46[0][0] = (-sinT) * sinP;
+    L.G46[0][1] = cosT * cosP;
+    L.G46[1][0] = sinT * cosP;
+    L.G46[1][1] = cosT * sinP;
+    L.G46[2][0] = 0.;
+    L.G46[2][1] = (-sinT);
+    const double ipdn = 1. / (L.dir[0] * D[0] + L.dir[1] * D[1] + L.dir[2] * D[2]);
+    double dP[3], dT[3];
+    const double cphi[3] = {L.G46[0][0], L.G46[1][0], L.G46[2][0]};
+    const double cth_[3] = {L.G46[0][1], L.G46[1][1], L.G46[2][1]};
+    cross3(Y, cphi, dP);
+    cross3(Y, cth_, dT);
+    const double xp = X[0] * dP[0] + X[1] * dP[1] + X[2] * dP[2];
+    const double xt = X[0] * dT[0] + X[1] * dT[1] + X[2] * dT[2];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      dP[r] = dP[r] - xp * X[r];
+      dT[r] = dT[r] - xt * X[r];
+      L.G03[r][2] = dP[r] * sp[0] * ipdn;
+      L.G03[r][3] = dT[r] * sp[0] * ipdn;
+    }
+  }
+  L.pc = PC_PRE;
+  navStatus(L, P, planes);
+}
+
+} // namespace kfd

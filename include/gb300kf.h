@@ -1,0 +1,201 @@
+/*
+ * gb300kf.h — C ABI of the GB300-native Kalman track fitter.
+ *
+ * One call fits a batch of tracks: RK4 (Nystroem) propagation with transport
+ * Jacobian through the magnetic field, direct navigation over a sequence of
+ * plane surfaces, gain-matrix Kalman update on every hit, gain-matrix (RTS)
+ * smoothing, and back-propagation of the first smoothed state to the per-track
+ * perigee line surface.  It replaces the per-track call
+ *
+ *   Acts::KalmanFitter<P,U,S,O>::fit(sourcelinks, startParameters, kfOptions,
+ *                                    kfResult, surfaceSequence, nSurfaces)
+ *     reference: include/Fitter/KalmanFitter.hpp:716-768
+ *
+ * and its device twin fitOnDevice (include/Fitter/KalmanFitter.hpp:790-850),
+ * launched per track by fitKernelThreadPerTrack / fitKernelBlockPerTrack
+ * (Run/GPU/Kernels.cu:6-94).
+ *
+ * Conventions
+ *  - Units are the reference's native units: mm, GeV, e; time in mm (c = 1);
+ *    magnetic field in GeV/(e*mm) (1 T = 0.000299792458).
+ *  - Bound parameter order (reference eBoundLoc0..eBoundTime):
+ *      0 loc0, 1 loc1, 2 phi, 3 theta, 4 q/p, 5 t.
+ *  - Covariances are passed as the 21 upper-triangle elements of the 6x6
+ *    matrix, row-major: (0,0) (0,1) .. (0,5) (1,1) .. (1,5) .. (5,5).
+ *  - Per-track arrays are structure-of-arrays: element `row` of track `i`
+ *    lives at ptr[row * stride + i].  `stride` >= n_tracks.
+ *  - All data pointers in kf_inputs_t / kf_outputs_t / workspace are DEVICE
+ *    pointers (kf_fit_batch) or HOST pointers (kf_fit_batch_host).
+ *    kf_geometry_t and kf_config_t are always read from host memory at call
+ *    time; the grid of a kf_field_t must be a device pointer.
+ *  - Calls are stream-ordered and asynchronous; nothing is allocated inside a
+ *    call.  Concurrent calls on different streams need distinct workspaces.
+ *  - Return codes: 0 on success, a negative kf_error on an API or CUDA error
+ *    (text via kf_last_error_string()).  The library never exits the process.
+ */
+#ifndef GB300KF_H
+#define GB300KF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KF_ABI_VERSION 1
+#define KF_MAX_PLANES 64 /* surfaces in one sequence */
+
+/* ---- call-level error codes (negative) ---------------------------------- */
+enum kf_error {
+  KF_SUCCESS = 0,
+  KF_ERR_INVALID_ARGUMENT = -1,
+  KF_ERR_WORKSPACE_TOO_SMALL = -2,
+  KF_ERR_CUDA = -3,
+  KF_ERR_UNSUPPORTED = -4,
+  KF_ERR_NO_DEVICE = -5
+};
+
+/* ---- per-track status (kf_outputs_t.status) ------------------------------ *
+ * KF_TRACK_OK corresponds to the reference fit() returning true; every other
+ * value to it returning false (KalmanFitter.hpp:760-767), with the cause.   */
+enum kf_track_status {
+  KF_TRACK_OK = 0,
+  KF_TRACK_MEAS_MISMATCH = 1, /* measurement states != hits on the track */
+  KF_TRACK_SMOOTHER_NAN = 2,  /* smoothing gain had a NaN (GainMatrixSmoother.hpp:63-66) */
+  KF_TRACK_MAX_STEPS = 3,     /* propagation hit maxSteps without the aborter */
+  KF_TRACK_NO_HITS = 4,       /* no measurement on the track */
+  KF_TRACK_BAD_INPUT = 5,     /* q/p == 0 or non-finite start parameters */
+  KF_TRACK_NOT_FITTED = 6     /* target surface never reached */
+};
+
+enum kf_precision {
+  KF_PRECISION_FP64 = 0, /* plain form: FP64 throughout */
+  KF_PRECISION_MIXED = 1 /* FP32 RK4/field/transport, FP64 gain/update/smoother */
+};
+
+enum kf_field_kind { KF_FIELD_CONSTANT = 0, KF_FIELD_GRID3D = 1 };
+
+enum kf_kernel_kind {
+  KF_KERNEL_AUTO = 0,
+  KF_KERNEL_THREAD_PER_TRACK = 1, /* one thread per track, grid over tracks */
+  KF_KERNEL_PERSISTENT = 2        /* persistent CTAs pulling a sorted queue */
+};
+
+/* Steering of the fit: PropagatorOptions (Propagator.hpp:52-111) plus
+ * KalmanFitterOptions (KalmanFitter.hpp:48-96) plus launch shape. */
+typedef struct kf_config {
+  int32_t precision;         /* kf_precision */
+  int32_t max_steps;         /* PropagatorOptions::maxSteps (1000) */
+  int32_t max_rk_trials;     /* PropagatorOptions::maxRungeKuttaStepTrials (10000) */
+  int32_t smoothing;         /* KalmanFitterOptions::smoothing (1) */
+  double tolerance;          /* RK error tolerance, PropagatorOptions::tolerance (1e-4) */
+  double step_size_cutoff;   /* PropagatorOptions::stepSizeCutOff (0) */
+  double mass;               /* particle mass used in dt/ds; the reference fit
+                                never sets it, so the muon default applies
+                                (Propagator.hpp:73): 0.1056583755 GeV */
+  double overstep_limit;     /* EigenStepper::m_overstepLimit (0.01 mm) */
+  double on_surface_tol;     /* s_onSurfaceTolerance (1e-4 mm) */
+  double outlier_chi2_cut;   /* > 0: hits whose predicted chi2 exceeds it are
+                                outliers (no update); 0 = off, as in the
+                                reference's VoidOutlierFinder */
+  int32_t faithful_jacobian; /* 1: keep the reference's jacToGlobal (not rebuilt
+                                after the update, EigenStepper.ipp:554-564);
+                                0: rebuild it at the updated state */
+  int32_t kernel;            /* kf_kernel_kind */
+  int32_t block_size;        /* threads per block; 0 = tuned default */
+  int32_t reserved0;
+} kf_config_t;
+
+/* The surface sequence: boundless plane surfaces (PlaneSurface<InfiniteBounds>,
+ * Surfaces/detail/PlaneSurface.ipp:24-69), in navigation order. */
+typedef struct kf_geometry {
+  int32_t n_planes;   /* <= KF_MAX_PLANES */
+  int32_t reserved0;
+  const double *center;   /* [n_planes][3] host memory */
+  const double *rotation; /* [n_planes][9] host memory, row-major 3x3 whose
+                             columns are the local axes U, V and the normal T */
+} kf_geometry_t;
+
+/* Magnetic field: Test::ConstantBField (include/Test/Helper.hpp:17-22) or an
+ * equidistant 3D grid with trilinear interpolation
+ * (MagneticField/InterpolatedBFieldMap.hpp:87-208). */
+typedef struct kf_field {
+  int32_t kind;             /* kf_field_kind */
+  int32_t nx, ny, nz;       /* grid points per axis (grid only) */
+  double value[3];          /* constant field (constant only) */
+  double scale;             /* global multiplier applied to every lookup */
+  double min[3], max[3];    /* grid extent in mm: point i at min + i*(max-min)/(n-1) */
+  const float *grid;        /* DEVICE [nz][ny][nx][4] = (bx, by, bz, 0) in
+                               GeV/(e*mm); index ((iz*ny)+iy)*nx+ix */
+} kf_field_t;
+
+/* Per-track inputs (structure of arrays). */
+typedef struct kf_inputs {
+  int64_t n_tracks;
+  int64_t stride;             /* elements between SoA rows, >= n_tracks */
+  int32_t n_surfaces;         /* planes in the sequence (== geometry n_planes) */
+  int32_t reserved0;
+  const double *meas;         /* [n_surfaces][5][stride]: loc0, loc1, var0,
+                                 cov01, var1 of the 2D pixel measurement
+                                 (EventData/PixelSourceLink.hpp:22-75) */
+  const uint64_t *hit_mask;   /* [stride] bit k set: plane k has a hit;
+                                 NULL: every plane has a hit */
+  const int32_t *n_planes;    /* [stride] length of the track's surface sequence
+                                 (first n planes); NULL: n_surfaces */
+  const double *start_params; /* [6][stride] bound parameters on the perigee line */
+  const double *start_cov;    /* [21][stride] upper triangle */
+  const double *perigee;      /* [3][stride] centre of the perigee line surface
+                                 (LineSurface with axis z, Run/Common/Processor.hpp:121-129) */
+} kf_inputs_t;
+
+/* Per-track outputs (structure of arrays). */
+typedef struct kf_outputs {
+  double *params;     /* [6][stride] fitted parameters at the perigee line */
+  double *cov;        /* [21][stride] their covariance */
+  double *chi2;       /* [stride] sum of predicted-residual chi2 over updates */
+  int32_t *status;    /* [stride] kf_track_status */
+  int32_t *n_meas;    /* [stride] measurement states (hits incl. outliers) */
+  int32_t *n_steps;   /* [stride] accepted RK steps (may be NULL) */
+  int32_t *n_trials;  /* [stride] RK4 stage evaluations incl. rejected trials
+                         (may be NULL) */
+  double *smoothed;   /* [n_surfaces][27][stride] smoothed parameters (6) and
+                         covariance (21) per measurement state; may be NULL */
+} kf_outputs_t;
+
+/* Version and diagnostics. */
+int32_t kf_version(void);
+const char *kf_last_error_string(void);
+
+/* Default configuration (reference defaults, FP64). */
+void kf_config_default(kf_config_t *cfg);
+
+/* Device workspace bytes kf_fit_batch needs for this batch shape. */
+size_t kf_workspace_size(const kf_config_t *cfg, int64_t n_tracks,
+                         int32_t n_surfaces);
+
+/* Fit a batch; all kf_inputs_t/kf_outputs_t pointers are device pointers.
+ * `stream` is a cudaStream_t (NULL = legacy default stream). */
+int32_t kf_fit_batch(const kf_inputs_t *in, kf_outputs_t *out,
+                     const kf_config_t *cfg, const kf_geometry_t *geo,
+                     const kf_field_t *field, void *workspace,
+                     size_t workspace_bytes, void *stream);
+
+/* Device bytes kf_fit_batch_host needs: workspace plus staging of inputs and
+ * outputs. */
+size_t kf_host_staging_size(const kf_config_t *cfg, int64_t n_tracks,
+                            int32_t n_surfaces, int32_t with_smoothed);
+
+/* Fit a batch held in HOST memory (pinned memory gives async copies): copies
+ * inputs into `device_staging`, fits, copies the outputs back, all on
+ * `stream`.  Blocks until the results are on the host. */
+int32_t kf_fit_batch_host(const kf_inputs_t *host_in, kf_outputs_t *host_out,
+                          const kf_config_t *cfg, const kf_geometry_t *geo,
+                          const kf_field_t *field, void *device_staging,
+                          size_t staging_bytes, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GB300KF_H */

@@ -1,0 +1,134 @@
+"""GPU parity: the CUDA fitter (through the C ABI) against the oracle.
+
+Tolerance: 1e-9 relative on fitted parameters (scale max(|x|, sigma_x)),
+covariance elements (scale sqrt(C_ii C_jj)) and chi2 (scale max(chi2, 1));
+status, measurement count and RK step count must be identical.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_close
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-9
+DIAG = [0, 6, 11, 15, 18, 20]
+
+
+def _compare(g, o, tol=TOL):
+    assert np.array_equal(g["status"], o["status"]), np.nonzero(g["status"] != o["status"])
+    assert np.array_equal(g["n_meas"], o["n_meas"])
+    assert np.array_equal(g["n_steps"], o["n_steps"])
+    assert np.array_equal(g["n_trials"], o["n_trials"])
+    ok = o["status"] == 0
+    worst = rel_close(g, o, tol, mask=ok)
+    assert worst <= 1.0, f"worst relative deviation {worst * tol:.3e} > {tol}"
+    return worst
+
+
+@pytest.mark.parametrize("overstep", [0.01, 0.1])
+def test_config0_parity(kf, orc, overstep):
+    """1000 tracks, 10-plane telescope, uniform 2 T (reference -d cpu -t 1000).
+    At the reference's 0.01 mm overstep limit a quarter of the tracks skip
+    planes and run to maxSteps: those paths must match too."""
+    tel = kf.make_telescope(1000)
+    cfg = kf.default_config(overstep_limit=overstep)
+    g = kf.fit_device(tel, cfg)
+    o = orc.fit(tel, cfg, threads=0)
+    _compare(g, o)
+    if overstep == 0.1:
+        assert np.all(g["status"] == 0)
+
+
+def test_host_api_matches_device_api(kf):
+    tel = kf.make_telescope(777)
+    cfg = kf.default_config(overstep_limit=0.1)
+    a = kf.fit_device(tel, cfg, smoothed=True)
+    b = kf.fit_host(tel, cfg, smoothed=True)
+    for k in ("params", "cov", "chi2", "status", "n_meas", "n_steps", "smoothed"):
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_smoothed_states_parity(kf, orc):
+    tel = kf.make_telescope(300)
+    cfg = kf.default_config(overstep_limit=0.1)
+    g = kf.fit_device(tel, cfg, smoothed=True)
+    o = orc.fit(tel, cfg, threads=0, smoothed=True)
+    sg, so = g["smoothed"], o["smoothed"]
+    for k in range(tel.n_surfaces):
+        sig = np.sqrt(so[k, 6 + np.array(DIAG)])
+        scale = np.maximum(np.abs(so[k, :6]), sig)
+        assert np.max(np.abs(sg[k, :6] - so[k, :6]) / scale) < TOL
+        assert np.max(np.abs(sg[k, 6 + 0] - so[k, 6 + 0]) / so[k, 6]) < TOL
+
+
+def test_config1_100k_parity(kf, orc):
+    tel = kf.make_telescope(100_000, seed=42)
+    cfg = kf.default_config(overstep_limit=0.1)
+    g = kf.fit_device(tel, cfg)
+    o = orc.fit(tel, cfg, threads=0)
+    _compare(g, o)
+
+
+def test_faithful_and_rebuilt_jacobian(kf, orc):
+    tel = kf.make_telescope(500, seed=3)
+    for faithful in (1, 0):
+        cfg = kf.default_config(overstep_limit=0.1, faithful_jacobian=faithful)
+        _compare(kf.fit_device(tel, cfg), orc.fit(tel, cfg, threads=0))
+
+
+def test_holes_outliers_parity(kf, orc):
+    tel = kf.make_telescope(20_000, n_planes=30, x_first=50., x_step=50., min_len=5, max_len=30,
+                           hit_prob=0.9, outlier_prob=0.02, seed=11)
+    cfg = kf.default_config(overstep_limit=0.1, outlier_chi2_cut=25.0)
+    _compare(kf.fit_device(tel, cfg), orc.fit(tel, cfg, threads=0))
+
+
+def test_field_map_parity(kf, orc):
+    tel = kf.make_telescope(3000, n_planes=30, x_first=50., x_step=50., field_map=True, seed=5)
+    cfg = kf.default_config(overstep_limit=0.1)
+    _compare(kf.fit_device(tel, cfg), orc.fit(tel, cfg, threads=0))
+
+
+def test_edge_cases(kf, orc):
+    cfg = kf.default_config(overstep_limit=0.1)
+    for n in (1, 31, 33, 129):
+        tel = kf.make_telescope(n, seed=n)
+        _compare(kf.fit_device(tel, cfg), orc.fit(tel, cfg, threads=1))
+    tel = kf.make_telescope(64, seed=9)
+    tel.start[4, 0] = 0.0
+    tel.start[2, 1] = np.nan
+    tel.hit_mask[2] = 0
+    tel.hit_mask[3] = 1          # a single hit
+    tel.n_planes[4] = 1
+    g = kf.fit_device(tel, cfg)
+    o = orc.fit(tel, cfg, threads=1)
+    assert g["status"][0] == 5 and g["status"][1] == 5 and g["status"][2] == 4
+    _compare(g, o)
+
+
+def test_empty_batch(kf):
+    tel = kf.make_telescope(1)
+    b = kf.DeviceBatch(tel, kf.default_config())
+    b.ins.n_tracks = 0
+    b.fit()  # no launch, no error
+
+
+def test_full_size_properties(kf):
+    """1M tracks: every track fits, pulls have unit width, reruns are bitwise
+    identical."""
+    import torch
+    tel = kf.make_telescope(1_000_000, seed=2024)
+    cfg = kf.default_config(overstep_limit=0.1)
+    b = kf.DeviceBatch(tel, cfg)
+    b.fit()
+    r1 = b.results()
+    b.fit()
+    torch.cuda.synchronize()
+    r2 = b.results()
+    for k in ("params", "cov", "chi2", "status", "n_steps"):
+        assert np.array_equal(r1[k], r2[k])
+    assert np.all(r1["status"] == 0)
+    pulls = (r1["params"] - tel.truth) / np.sqrt(r1["cov"][DIAG])
+    assert np.all(np.abs(pulls[:5].std(axis=1) - 1) < 0.02)
+    assert abs(r1["chi2"].mean() / 20 - 1) < 0.01

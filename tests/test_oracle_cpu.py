@@ -1,0 +1,184 @@
+"""CPU tests of the oracle (the FP64 restatement of the reference fitter).
+
+The reference ships no tests, golden vectors or fixtures and cannot be built
+here (Eigen3, Boost and ROOT are absent), so the oracle is pinned by
+known-answer tests instead: the exact helix, finite-difference transport
+Jacobians, a direct least-squares solve of the Kalman algebra, pull widths,
+and the reference's own overstep behaviour on this workload.
+"""
+import numpy as np
+import pytest
+
+DIAG = [0, 6, 11, 15, 18, 20]
+
+
+def _tiny_errors(kf, n, **kw):
+    return kf.make_telescope(n, hit_sigma=1e-9, seed_loc_sigma=1e-9, seed_angle_sigma=1e-9,
+                             seed_qop_rel=1e-9, seed_time_sigma=1e-9, **kw)
+
+
+def test_rk_propagation_matches_exact_helix(kf, orc):
+    # every hit treated as an outlier: pure propagation from the true seed;
+    # the generator's hits are the exact helix (uniform 2 T)
+    tel = _tiny_errors(kf, 1000)
+    cfg = kf.default_config(overstep_limit=0.1, outlier_chi2_cut=1e-300)
+    o = orc.fit(tel, cfg, threads=4, states=True)
+    d = np.abs(o["states"][:, :2, :] - tel.meas[:, :2, :])
+    assert np.all(o["n_meas"] == 10)
+    assert d.max() < 1e-4, d.max()     # RK4 with 1e-4 tolerance over 1 m
+
+
+def _prop_states(kf, orc, tel, cfg):
+    return orc.fit(tel, cfg, threads=1, states=True)["states"]
+
+
+def test_transport_jacobian_against_finite_differences(kf, orc):
+    tel = _tiny_errors(kf, 8)
+    cfg = kf.default_config(overstep_limit=0.1, outlier_chi2_cut=1e-300)
+    base = _prop_states(kf, orc, tel, cfg)
+    S = tel.n_surfaces
+    # full Jacobian to plane k = J_k ... J_0
+    jac = base[:, 27:63, :].reshape(S, 6, 6, tel.n)
+    eps = np.array([1e-4, 1e-4, 1e-7, 1e-7, 0.0, 1e-3])
+    for t in range(tel.n):
+        eps[4] = 1e-7 * abs(tel.start[4, t])
+        full = np.eye(6)
+        fds = {}
+        for j in range(6):
+            plus, minus = tel.start.copy(), tel.start.copy()
+            plus[j, t] += eps[j]
+            minus[j, t] -= eps[j]
+            tp = kf.Telescope(**{**tel.__dict__, "start": plus})
+            tm = kf.Telescope(**{**tel.__dict__, "start": minus})
+            sp = _prop_states(kf, orc, tp, cfg)
+            sm = _prop_states(kf, orc, tm, cfg)
+            fds[j] = (sp[:, :6, t] - sm[:, :6, t]) / (2 * eps[j])
+        for k in range(S):
+            full = jac[k, :, :, t] @ full
+            fd = np.stack([fds[j][k] for j in range(6)], axis=1)
+            for r in range(5):
+                for c in range(5):
+                    scale = max(abs(full[r, c]), 1e-3 * np.abs(full[r]).max(), 1e-12)
+                    assert abs(fd[r, c] - full[r, c]) <= 2e-4 * scale + 1e-9, (t, k, r, c, fd[r, c], full[r, c])
+
+
+def test_kalman_algebra_equals_least_squares(kf, orc):
+    """Straight tracks (B ~ 0): the smoothed perigee estimate is the linear
+    Gaussian posterior of the seed prior and the plane measurements."""
+    n = 40
+    tel = kf.make_telescope(n, n_planes=3, bz_tesla=1e-12)
+    cfg = kf.default_config(overstep_limit=0.1)
+    o = orc.fit(tel, cfg, threads=2)
+    assert np.all(o["status"] == 0)
+    X = tel.center[:, 0]
+    for t in range(n):
+        c = tel.perigee[:, t]
+
+        def f(x):
+            d0, z0, phi, th = x
+            dvec = np.array([np.cos(phi) * np.sin(th), np.sin(phi) * np.sin(th), np.cos(th)])
+            mx = np.cross([0, 0, 1], dvec)
+            mx /= np.linalg.norm(mx)
+            p0 = c + d0 * mx + np.array([0, 0, z0])
+            out = []
+            for xk in X:
+                s = (xk - p0[0]) / dvec[0]
+                out += [p0[1] + s * dvec[1], p0[2] + s * dvec[2]]
+            return np.array(out)
+
+        x0 = tel.start[:4, t]
+        C0 = np.diag([tel.start_cov[DIAG[i], t] for i in range(4)])
+        m = tel.meas[:, :2, t].reshape(-1)
+        V = np.diag(np.repeat(tel.meas[:, 2, t], 2))
+        x = x0.copy()
+        for _ in range(5):  # Gauss-Newton on the exact straight-line model
+            A = np.zeros((2 * len(X), 4))
+            for j in range(4):
+                h = np.zeros(4)
+                h[j] = 1e-6 if j < 2 else 1e-8
+                A[:, j] = (f(x + h) - f(x - h)) / (2 * h[j])
+            P = np.linalg.inv(np.linalg.inv(C0) + A.T @ np.linalg.inv(V) @ A)
+            x = x + P @ (A.T @ np.linalg.inv(V) @ (m - f(x)) - np.linalg.inv(C0) @ (x - x0))
+        sig = np.sqrt(np.diag(P))
+        got = o["params"][:4, t]
+        assert np.all(np.abs(got - x) < 1e-3 * sig), (t, got, x, sig)
+        gcov = np.array([[o["cov"][kf_idx(i, j), t] for j in range(4)] for i in range(4)])
+        assert np.allclose(gcov, P, rtol=1e-3, atol=1e-3 * np.outer(sig, sig).max()), (gcov, P)
+
+
+def kf_idx(i, j):
+    i, j = min(i, j), max(i, j)
+    return i * 6 - (i * (i - 1)) // 2 + (j - i)
+
+
+def test_pull_widths_and_chi2(kf, orc):
+    tel = kf.make_telescope(20000)
+    o = orc.fit(tel, kf.default_config(overstep_limit=0.1), threads=0)
+    ok = o["status"] == 0
+    assert ok.all()
+    pulls = (o["params"] - tel.truth) / np.sqrt(o["cov"][DIAG])
+    width = pulls[:5].std(axis=1)
+    assert np.all(np.abs(width - 1) < 0.04), width
+    assert np.all(np.abs(pulls[:5].mean(axis=1)) < 0.05)
+    ndf = 2 * 10
+    assert abs(o["chi2"].mean() / ndf - 1) < 0.03
+
+
+def test_reference_overstep_limit_skips_planes(kf, orc):
+    """At the reference's fixed 0.01 mm overstep limit, tracks bending towards
+    the plane normal overshoot planes by more than the limit; the navigator
+    then skips the planes and the fit fails (KalmanFitter.hpp:760-764)."""
+    tel = kf.make_telescope(2000)
+    o = orc.fit(tel, kf.default_config(), threads=0)
+    bad = o["status"] != 0
+    assert 0.1 < bad.mean() < 0.45
+    assert np.all(o["status"][bad] == 1)
+    # failures are high-momentum tracks turning towards +x (q*phi > 0 in +Bz)
+    q = np.sign(tel.truth[4])
+    turning_in = q * tel.truth[2] > 0
+    assert turning_in[bad].mean() > 0.95
+
+
+def test_oracle_independent_of_threads(kf, orc):
+    tel = kf.make_telescope(500, n_planes=12, min_len=6, max_len=12, hit_prob=0.9,
+                           outlier_prob=0.05)
+    cfg = kf.default_config(overstep_limit=0.1, outlier_chi2_cut=30.0)
+    a = orc.fit(tel, cfg, threads=1)
+    b = orc.fit(tel, cfg, threads=4)
+    for k in ("params", "cov", "chi2", "status", "n_steps"):
+        assert np.array_equal(a[k], b[k])
+
+
+def test_holes_and_outliers(kf, orc):
+    tel = kf.make_telescope(3000, n_planes=30, x_first=50., x_step=50., min_len=5, max_len=30,
+                           hit_prob=0.9, outlier_prob=0.02)
+    cfg = kf.default_config(overstep_limit=0.1, outlier_chi2_cut=25.0)
+    o = orc.fit(tel, cfg, threads=0)
+    ok = o["status"] == 0
+    hits = np.array([bin(int(m) & ((1 << int(L)) - 1)).count("1")
+                     for m, L in zip(tel.hit_mask, tel.n_planes)])
+    assert np.array_equal(o["n_meas"][ok], hits[ok])
+    assert ok.mean() > 0.99
+    pulls = ((o["params"] - tel.truth) / np.sqrt(np.abs(o["cov"][DIAG])))[:5, ok]
+    w = np.median(np.abs(pulls), axis=1) / 0.6745
+    assert np.all(np.abs(w - 1) < 0.1), w
+
+
+def test_field_map_fit(kf, orc):
+    tel = kf.make_telescope(1000, n_planes=30, x_first=50., x_step=50., field_map=True,
+                           field_n=41)
+    o = orc.fit(tel, kf.default_config(overstep_limit=0.1), threads=0)
+    ok = o["status"] == 0
+    assert ok.mean() > 0.99
+    pulls = ((o["params"] - tel.truth) / np.sqrt(o["cov"][DIAG]))[:5, ok]
+    assert np.all(np.abs(pulls.std(axis=1) - 1) < 0.1), pulls.std(axis=1)
+
+
+def test_bad_inputs_and_no_hits(kf, orc):
+    tel = kf.make_telescope(8)
+    tel.start[4, 0] = 0.0
+    tel.start[2, 1] = np.nan
+    tel.hit_mask[2] = 0
+    o = orc.fit(tel, kf.default_config(overstep_limit=0.1), threads=1)
+    assert o["status"][0] == 5 and o["status"][1] == 5 and o["status"][2] == 4
+    assert np.all(o["status"][3:] == 0)
