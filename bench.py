@@ -202,7 +202,7 @@ def run_gpu(args) -> None:
     dense_flop = F.batch_flops(res["n_trials"], res["n_steps"], res["n_meas"], res["status"], dense=True)
     avg_launch_s = statistics.mean(launch_ms) * 1e-3
     peak = C.c_double(0)
-    rc = lib.kf_diag_fp64_fma_rate(C.c_int32(200000), C.byref(peak), C.c_void_p(stream.cuda_stream))
+    rc = lib.kf_diag_fp64_fma_rate(C.c_int32(20000), C.byref(peak), C.c_void_p(stream.cuda_stream))
     peak_tflops = peak.value / 1e3 if rc == 0 else None
     achieved = flop / avg_launch_s / 1e12
     traffic = None

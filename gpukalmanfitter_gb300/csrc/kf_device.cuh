@@ -30,11 +30,12 @@
 
 namespace kfd {
 
-constexpr int kStateStride = 79; // doubles per stored measurement state
+constexpr int kStateStride = 37; // doubles per stored measurement state
 // layout of one stored state (smoother input):
-//   [0,6) predicted params, [6,27) predicted cov (upper),
-//   [27,33) filtered params, [33,54) filtered cov, [54,79) jacobian rows
-//   0..3 cols 0..4 (20) and row 5 cols 0..4 (5)
+//   [0,6) predicted params, [6,12) filtered params, [12,37) bound-to-bound
+//   jacobian from the previous state: rows 0..3 cols 0..4 (20) and row 5
+//   cols 0..4 (5); the other entries are structural (row 4 = e4, column
+//   5 = e5).  The smoother needs no stored covariance (see finalizeSmooth).
 
 struct PlaneD {
   double c[3], U[3], V[3], T[3];
@@ -657,18 +658,15 @@ __device__ void filterHit(Lane &L, const Params &P, const PlaneD *planes, int k)
   const bool outlier = (P.outlierCut > 0. && chi2 > P.outlierCut);
   const int s = L.measStates;
   if (s == 0) L.firstPlane = k;
-  // store predicted state and Jacobian
+  // store predicted parameters and the Jacobian
 #pragma unroll
   for (int e = 0; e < 6; ++e) *wsPtr(P, L, s, e) = pred[e];
 #pragma unroll
-  for (int e = 0; e < 21; ++e) *wsPtr(P, L, s, 6 + e) = L.cov[e];
-#pragma unroll
-  for (int e = 0; e < 25; ++e) *wsPtr(P, L, s, 54 + e) = Jst[e];
+  for (int e = 0; e < 25; ++e) *wsPtr(P, L, s, 12 + e) = Jst[e];
   if (outlier) {
+    // filtered = predicted; the stepper keeps the predicted state
 #pragma unroll
-    for (int e = 0; e < 6; ++e) *wsPtr(P, L, s, 27 + e) = pred[e];
-#pragma unroll
-    for (int e = 0; e < 21; ++e) *wsPtr(P, L, s, 33 + e) = L.cov[e];
+    for (int e = 0; e < 6; ++e) *wsPtr(P, L, s, 6 + e) = pred[e];
   } else {
     double K0[6], K1[6];
 #pragma unroll
@@ -687,9 +685,7 @@ __device__ void filterHit(Lane &L, const Params &P, const PlaneD *planes, int k)
         cf[ut(i, j)] = L.cov[ut(i, j)] - K0[i] * L.cov[sidx(0, j)] - K1[i] * L.cov[sidx(1, j)];
     }
 #pragma unroll
-    for (int e = 0; e < 6; ++e) *wsPtr(P, L, s, 27 + e) = filt[e];
-#pragma unroll
-    for (int e = 0; e < 21; ++e) *wsPtr(P, L, s, 33 + e) = cf[e];
+    for (int e = 0; e < 6; ++e) *wsPtr(P, L, s, 6 + e) = filt[e];
     L.chi2 += chi2;
     stepperUpdate(L, pl, filt, cf, P.mass);
     if (!P.faithful) planeJacToGlobal(L, pl);
@@ -697,62 +693,92 @@ __device__ void filterHit(Lane &L, const Params &P, const PlaneD *planes, int k)
   L.measStates++;
 }
 
-// Symmetric 6x6 inverse by LDL^T (the predicted covariance is positive
-// definite); input and output upper triangles.
-__device__ __forceinline__ void invSym6(const double A[21], double Inv[21]) {
-  double Lm[6][6], d[6], rd[6];
+// Inverse of the structured bound-to-bound Jacobian
+//   J = [[A, b, 0], [0, 1, 0], [c, d, 1]]   (A 4x4, blocks loc/angles, q/p, t)
+//   J^-1 = [[A^-1, -A^-1 b, 0], [0, 1, 0], [-c A^-1, -d + c A^-1 b, 1]]
+// with A^-1 from its 2x2 blocks (Schur complement).  Output rows 0..3 and 5,
+// cols 0..4, in the stored-Jacobian layout.
+__device__ __forceinline__ void invJacobian(const double J[25], double Gi[25]) {
+  const double p00 = J[0], p01 = J[1], p10 = J[5], p11 = J[6];
+  const double q00 = J[2], q01 = J[3], q10 = J[7], q11 = J[8];
+  const double r00 = J[10], r01 = J[11], r10 = J[15], r11 = J[16];
+  const double s00 = J[12], s01 = J[13], s10 = J[17], s11 = J[18];
+  const double rdp = 1. / (p00 * p11 - p01 * p10);
+  const double i00 = p11 * rdp, i01 = -p01 * rdp, i10 = -p10 * rdp, i11 = p00 * rdp;
+  // T = P^-1 Q, U = R P^-1
+  const double t00 = i00 * q00 + i01 * q10, t01 = i00 * q01 + i01 * q11;
+  const double t10 = i10 * q00 + i11 * q10, t11 = i10 * q01 + i11 * q11;
+  const double u00 = r00 * i00 + r01 * i10, u01 = r00 * i01 + r01 * i11;
+  const double u10 = r10 * i00 + r11 * i10, u11 = r10 * i01 + r11 * i11;
+  // S' = S - R T, Si = S'^-1
+  const double a00 = s00 - (r00 * t00 + r01 * t10), a01 = s01 - (r00 * t01 + r01 * t11);
+  const double a10 = s10 - (r10 * t00 + r11 * t10), a11 = s11 - (r10 * t01 + r11 * t11);
+  const double rds = 1. / (a00 * a11 - a01 * a10);
+  const double z00 = a11 * rds, z01 = -a01 * rds, z10 = -a10 * rds, z11 = a00 * rds;
+  double Ai[4][4];
+  // lower-right Si, lower-left -Si U, upper-right -T Si, upper-left P^-1 + T Si U
+  Ai[2][2] = z00;
+  Ai[2][3] = z01;
+  Ai[3][2] = z10;
+  Ai[3][3] = z11;
+  Ai[2][0] = -(z00 * u00 + z01 * u10);
+  Ai[2][1] = -(z00 * u01 + z01 * u11);
+  Ai[3][0] = -(z10 * u00 + z11 * u10);
+  Ai[3][1] = -(z10 * u01 + z11 * u11);
+  Ai[0][2] = -(t00 * z00 + t01 * z10);
+  Ai[0][3] = -(t00 * z01 + t01 * z11);
+  Ai[1][2] = -(t10 * z00 + t11 * z10);
+  Ai[1][3] = -(t10 * z01 + t11 * z11);
+  Ai[0][0] = i00 - (t00 * Ai[2][0] + t01 * Ai[3][0]);
+  Ai[0][1] = i01 - (t00 * Ai[2][1] + t01 * Ai[3][1]);
+  Ai[1][0] = i10 - (t10 * Ai[2][0] + t11 * Ai[3][0]);
+  Ai[1][1] = i11 - (t10 * Ai[2][1] + t11 * Ai[3][1]);
+  const double b[4] = {J[4], J[9], J[14], J[19]};
+  const double c[4] = {J[20], J[21], J[22], J[23]};
+  const double d = J[24];
+  double cb = 0.;
 #pragma unroll
-  for (int j = 0; j < 6; ++j) {
-    double v = A[ut(j, j)];
+  for (int r = 0; r < 4; ++r) {
+    double v = 0.;
 #pragma unroll
-    for (int k = 0; k < j; ++k) v -= Lm[j][k] * Lm[j][k] * d[k];
-    d[j] = v;
-    rd[j] = 1. / v;
+    for (int k = 0; k < 4; ++k) v += Ai[r][k] * b[k];
 #pragma unroll
-    for (int i = j + 1; i < 6; ++i) {
-      double w = A[ut(j, i)];
-#pragma unroll
-      for (int k = 0; k < j; ++k) w -= Lm[i][k] * Lm[j][k] * d[k];
-      Lm[i][j] = w * rd[j];
-    }
+    for (int k = 0; k < 4; ++k) Gi[5 * r + k] = Ai[r][k];
+    Gi[5 * r + 4] = -v;
+    cb += c[r] * v;
   }
-  // Y = L^-1 (unit lower)
-  double Y[6][6];
 #pragma unroll
-  for (int i = 0; i < 6; ++i) {
+  for (int k = 0; k < 4; ++k) {
+    double v = 0.;
 #pragma unroll
-    for (int j = 0; j < i; ++j) {
-      double v = -Lm[i][j];
-#pragma unroll
-      for (int k = j + 1; k < i; ++k) v -= Lm[i][k] * Y[k][j];
-      Y[i][j] = v;
-    }
+    for (int r = 0; r < 4; ++r) v += c[r] * Ai[r][k];
+    Gi[20 + k] = -v;
   }
-  // Inv = Y^T D^-1 Y
-#pragma unroll
-  for (int i = 0; i < 6; ++i) {
-#pragma unroll
-    for (int j = i; j < 6; ++j) {
-      double v = rd[j] * ((j == i) ? 1. : Y[j][i]);
-#pragma unroll
-      for (int k = j + 1; k < 6; ++k) v += Y[k][i] * rd[k] * Y[k][j];
-      Inv[ut(i, j)] = v;
-    }
-  }
+  Gi[24] = -d + cb;
 }
 
 // ---------------------------------------------------------------------------
-// Actor::finalize (KalmanFitter.hpp:360-393) with GainMatrixSmoother
-// (GainMatrixSmoother.hpp:21-94).  Returns false on a NaN gain.
+// Actor::finalize (KalmanFitter.hpp:360-393) with the gain-matrix (RTS)
+// smoother (GainMatrixSmoother.hpp:21-94).  Returns false on a NaN gain.
+//
+// The reference gain is G = C_f J^T C_p'^-1 with C_p' = J C_f J^T the
+// predicted covariance of the next state.  On this path (no material, no
+// process noise) that product is exactly J^-1, and the smoothed covariance
+// C_s = C_f - G (C_p' - C_s') G^T reduces to G C_s' G^T.  The kernel uses
+// these closed forms: the same quantities in exact arithmetic, without the
+// cancellation of the reference form (whose q/p variance moves by 1e-9 to
+// 5e-8 relative between two valid FP64 evaluations), and without storing
+// covariances per state.
 // ---------------------------------------------------------------------------
 __device__ bool finalizeSmooth(Lane &L, const Params &P, const PlaneD *planes) {
   L.smoothed = true;
   const int n = L.measStates;
   double xs[6], Cs[21];
 #pragma unroll
-  for (int e = 0; e < 6; ++e) xs[e] = *wsPtr(P, L, n - 1, 27 + e);
+  for (int e = 0; e < 6; ++e) xs[e] = *wsPtr(P, L, n - 1, 6 + e);
+  // the stepper holds the last filtered covariance
 #pragma unroll
-  for (int e = 0; e < 21; ++e) Cs[e] = *wsPtr(P, L, n - 1, 33 + e);
+  for (int e = 0; e < 21; ++e) Cs[e] = L.cov[e];
   if (P.oSmoothed) {
 #pragma unroll
     for (int e = 0; e < 6; ++e)
@@ -762,83 +788,68 @@ __device__ bool finalizeSmooth(Lane &L, const Params &P, const PlaneD *planes) {
       P.oSmoothed[((size_t)(n - 1) * 27 + 6 + e) * P.stride + L.idx] = Cs[e];
   }
   for (int i = n - 2; i >= 0; --i) {
-    double xp[6], Cp[21], Jn[25], xf[6], Cf[21];
+    double xp[6], Jn[25], xf[6], G[25];
 #pragma unroll
     for (int e = 0; e < 6; ++e) xp[e] = *wsPtr(P, L, i + 1, e);
 #pragma unroll
-    for (int e = 0; e < 21; ++e) Cp[e] = *wsPtr(P, L, i + 1, 6 + e);
+    for (int e = 0; e < 25; ++e) Jn[e] = *wsPtr(P, L, i + 1, 12 + e);
 #pragma unroll
-    for (int e = 0; e < 25; ++e) Jn[e] = *wsPtr(P, L, i + 1, 54 + e);
-#pragma unroll
-    for (int e = 0; e < 6; ++e) xf[e] = *wsPtr(P, L, i, 27 + e);
-#pragma unroll
-    for (int e = 0; e < 21; ++e) Cf[e] = *wsPtr(P, L, i, 33 + e);
-    double inv[21];
-    invSym6(Cp, inv);
-    // A = Cf J^T (J rows 0-3,5 have cols 0..4; row 4 = e4; col 5 = e5 on row 5)
-    double A[6][6];
-#pragma unroll
-    for (int r = 0; r < 6; ++r) {
-#pragma unroll
-      for (int c = 0; c < 6; ++c) {
-        if (c == 4) {
-          A[r][c] = Cf[sidx(r, 4)];
-        } else {
-          const int jr = (c == 5) ? 4 : c; // row of the stored Jacobian
-          double s = Cf[sidx(r, 0)] * Jn[5 * jr + 0];
-#pragma unroll
-          for (int k = 1; k < 5; ++k) s += Cf[sidx(r, k)] * Jn[5 * jr + k];
-          if (c == 5) s += Cf[sidx(r, 5)];
-          A[r][c] = s;
-        }
-      }
-    }
-    // G = A inv
-    double G[6][6];
+    for (int e = 0; e < 6; ++e) xf[e] = *wsPtr(P, L, i, 6 + e);
+    invJacobian(Jn, G);
     bool nan = false;
 #pragma unroll
-    for (int r = 0; r < 6; ++r) {
-#pragma unroll
-      for (int c = 0; c < 6; ++c) {
-        double s = A[r][0] * inv[sidx(0, c)];
-#pragma unroll
-        for (int k = 1; k < 6; ++k) s += A[r][k] * inv[sidx(k, c)];
-        G[r][c] = s;
-        nan = nan || (s != s);
-      }
-    }
+    for (int e = 0; e < 25; ++e) nan = nan || (G[e] != G[e]);
     if (nan) return false;
-    double dx[6], D[21];
+    double dx[6];
 #pragma unroll
     for (int e = 0; e < 6; ++e) dx[e] = xs[e] - xp[e];
-#pragma unroll
-    for (int e = 0; e < 21; ++e) D[e] = Cp[e] - Cs[e];
+    // rows 0..3 and 5 of G have columns 0..4 stored; row 4 = e4, G(5,5) = 1
 #pragma unroll
     for (int r = 0; r < 6; ++r) {
-      double g = G[r][0] * dx[0];
+      if (r == 4) {
+        xs[4] = xf[4] + dx[4];
+      } else {
+        const int gr = (r == 5) ? 4 : r;
+        double g = G[5 * gr] * dx[0];
 #pragma unroll
-      for (int k = 1; k < 6; ++k) g += G[r][k] * dx[k];
-      xs[r] = xf[r] + g;
+        for (int k = 1; k < 5; ++k) g += G[5 * gr + k] * dx[k];
+        if (r == 5) g += dx[5];
+        xs[r] = xf[r] + g;
+      }
     }
-    double W[6][6];
+    // Cs <- G Cs G^T
+    double M[6][6];
 #pragma unroll
     for (int r = 0; r < 6; ++r) {
 #pragma unroll
       for (int c = 0; c < 6; ++c) {
-        double s = G[r][0] * D[sidx(0, c)];
+        if (r == 4) {
+          M[r][c] = Cs[sidx(4, c)];
+        } else {
+          const int gr = (r == 5) ? 4 : r;
+          double v = G[5 * gr] * Cs[sidx(0, c)];
 #pragma unroll
-        for (int k = 1; k < 6; ++k) s += G[r][k] * D[sidx(k, c)];
-        W[r][c] = s;
+          for (int k = 1; k < 5; ++k) v += G[5 * gr + k] * Cs[sidx(k, c)];
+          if (r == 5) v += Cs[sidx(5, c)];
+          M[r][c] = v;
+        }
       }
     }
 #pragma unroll
     for (int r = 0; r < 6; ++r) {
 #pragma unroll
       for (int c = r; c < 6; ++c) {
-        double s = W[r][0] * G[c][0];
+        double v;
+        if (c == 4) {
+          v = M[r][4];
+        } else {
+          const int gc = (c == 5) ? 4 : c;
+          v = M[r][0] * G[5 * gc];
 #pragma unroll
-        for (int k = 1; k < 6; ++k) s += W[r][k] * G[c][k];
-        Cs[ut(r, c)] = Cf[ut(r, c)] - s;
+          for (int k = 1; k < 5; ++k) v += M[r][k] * G[5 * gc + k];
+          if (c == 5) v += M[r][5];
+        }
+        Cs[ut(r, c)] = v;
       }
     }
     if (P.oSmoothed) {

@@ -19,38 +19,50 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 SRC = HERE / "kf_oracle.cpp"
 LIB = HERE / "_build" / "libkforacle.so"
+# Same source with the smoother evaluated in extended precision (long double):
+# the comparison point for the GPU (see the note on the smoother in
+# kf_oracle.cpp).
+LIB_PRECISE = HERE / "_build" / "libkforacle_precise.so"
 HEADER = HERE.parent / "include" / "gb300kf.h"
 
-_LIB = None
+_LIBS: dict = {}
 
 
-def build(force: bool = False) -> Path:
-    if not force and LIB.exists() and LIB.stat().st_mtime >= max(SRC.stat().st_mtime,
-                                                                 HEADER.stat().st_mtime):
-        return LIB
-    LIB.parent.mkdir(parents=True, exist_ok=True)
-    tmp = LIB.with_suffix(".so.tmp")
-    cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
-           "-o", str(tmp), str(SRC)]
+def _compile(target: Path, flags: list[str], force: bool) -> Path:
+    if not force and target.exists() and target.stat().st_mtime >= max(SRC.stat().st_mtime,
+                                                                       HEADER.stat().st_mtime):
+        return target
+    target.parent.mkdir(parents=True, exist_ok=True)
+    tmp = target.with_suffix(".so.tmp")
+    cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", *flags, "-fPIC", "-shared", "-o", str(tmp),
+           str(SRC)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{res.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, target)
+    return target
 
 
-def load():
-    global _LIB
-    if _LIB is None:
-        build()
-        _LIB = C.CDLL(str(LIB))
-        _LIB.oracle_fit.restype = C.c_int32
-        _LIB.oracle_num_threads.restype = C.c_int32
-    return _LIB
+def build(force: bool = False, variant: str = "default") -> Path:
+    """Compile the oracle.  ``variant="precise"`` evaluates the smoother in
+    long double; the default build is FP64 throughout (the CPU baseline)."""
+    if variant == "precise":
+        return _compile(LIB_PRECISE, ["-ffp-contract=off", "-DKFO_SMOOTHER_REAL=long double"], force)
+    return _compile(LIB, ["-ffp-contract=off"], force)
+
+
+def load(variant: str = "default"):
+    if variant not in _LIBS:
+        lib = C.CDLL(str(build(variant=variant)))
+        lib.oracle_fit.restype = C.c_int32
+        lib.oracle_num_threads.restype = C.c_int32
+        _LIBS[variant] = lib
+    return _LIBS[variant]
 
 
 def fit(tel, cfg=None, *, threads: int = 0, smoothed: bool = False, masks: bool = True,
-        field_scale: float = 1.0, center=None, rotation=None, states: bool = False) -> dict:
+        field_scale: float = 1.0, center=None, rotation=None, states: bool = False,
+        variant: str = "default") -> dict:
     """Fit a Telescope workload on the host; returns the same arrays as the GPU.
 
     With ``states=True`` the result also holds ``states`` [S,63,n]: predicted
@@ -58,7 +70,7 @@ def fit(tel, cfg=None, *, threads: int = 0, smoothed: bool = False, masks: bool 
     Jacobian of every measurement state.
     """
     import gpukalmanfitter_gb300 as kf
-    lib = load()
+    lib = load(variant)
     cfg = cfg or kf.default_config()
     n, S = tel.n, tel.n_surfaces
     out = kf.host_outputs(n, S, smoothed)

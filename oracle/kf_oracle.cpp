@@ -726,6 +726,100 @@ static bool hasNaN(const Mat<6, 6> &m) {
 }
 
 // ---------------------------------------------------------------------------
+// Smoother arithmetic type.  The default build evaluates the reference
+// smoother in FP64, as the reference's double build does.  The "precise"
+// build (-DKFO_SMOOTHER_REAL="long double") evaluates the same formulas in
+// extended precision: the update C_s = C_f - G (C_p' - C_s') G^T cancels
+// heavily for the q/p variance, so FP64 evaluations of it scatter by 1e-9 to
+// 5e-8 relative; the extended evaluation is close to the formula's exact
+// value and is the comparison point for the GPU.
+// ---------------------------------------------------------------------------
+#ifndef KFO_SMOOTHER_REAL
+#define KFO_SMOOTHER_REAL double
+#endif
+typedef KFO_SMOOTHER_REAL SReal;
+struct M6 {
+  SReal a[6][6];
+};
+static M6 toM6(const Mat<6, 6> &m) {
+  M6 r;
+  for (int i = 0; i < 6; ++i)
+    for (int j = 0; j < 6; ++j) r.a[i][j] = m.a[i][j];
+  return r;
+}
+static Mat<6, 6> fromM6(const M6 &m) {
+  Mat<6, 6> r;
+  for (int i = 0; i < 6; ++i)
+    for (int j = 0; j < 6; ++j) r.a[i][j] = (double)m.a[i][j];
+  return r;
+}
+static M6 mul6(const M6 &A, const M6 &B) {
+  M6 r;
+  for (int i = 0; i < 6; ++i)
+    for (int j = 0; j < 6; ++j) {
+      SReal v = 0;
+      for (int k = 0; k < 6; ++k) v += A.a[i][k] * B.a[k][j];
+      r.a[i][j] = v;
+    }
+  return r;
+}
+static M6 tr6(const M6 &A) {
+  M6 r;
+  for (int i = 0; i < 6; ++i)
+    for (int j = 0; j < 6; ++j) r.a[j][i] = A.a[i][j];
+  return r;
+}
+static M6 sub6(const M6 &A, const M6 &B) {
+  M6 r;
+  for (int i = 0; i < 6; ++i)
+    for (int j = 0; j < 6; ++j) r.a[i][j] = A.a[i][j] - B.a[i][j];
+  return r;
+}
+// partial-pivot LU inverse (as inverse6) in the smoother type
+static M6 inverse6s(const M6 &M) {
+  SReal A[6][6];
+  int perm[6];
+  for (int i = 0; i < 6; ++i) {
+    perm[i] = i;
+    for (int j = 0; j < 6; ++j) A[i][j] = M.a[i][j];
+  }
+  for (int k = 0; k < 6; ++k) {
+    int piv = k;
+    SReal best = A[k][k] < 0 ? -A[k][k] : A[k][k];
+    for (int i = k + 1; i < 6; ++i) {
+      SReal v = A[i][k] < 0 ? -A[i][k] : A[i][k];
+      if (v > best) {
+        best = v;
+        piv = i;
+      }
+    }
+    if (piv != k) {
+      for (int j = 0; j < 6; ++j) std::swap(A[k][j], A[piv][j]);
+      std::swap(perm[k], perm[piv]);
+    }
+    for (int i = k + 1; i < 6; ++i) {
+      A[i][k] /= A[k][k];
+      for (int j = k + 1; j < 6; ++j) A[i][j] -= A[i][k] * A[k][j];
+    }
+  }
+  M6 inv;
+  for (int col = 0; col < 6; ++col) {
+    SReal y[6];
+    for (int i = 0; i < 6; ++i) {
+      SReal v = (perm[i] == col) ? 1 : 0;
+      for (int j = 0; j < i; ++j) v -= A[i][j] * y[j];
+      y[i] = v;
+    }
+    for (int i = 5; i >= 0; --i) {
+      SReal v = y[i];
+      for (int j = i + 1; j < 6; ++j) v -= A[i][j] * inv.a[j][col];
+      inv.a[i][col] = v / A[i][i];
+    }
+  }
+  return inv;
+}
+
+// ---------------------------------------------------------------------------
 // The fit of one track: KalmanFitter::fit (Fitter/KalmanFitter.hpp:716-768)
 // driving Propagator::propagate (Propagator/Propagator.ipp:6-96) with the
 // Kalman actor (KalmanFitter.hpp:216-393), the Kalman aborter (:682-694),
@@ -911,19 +1005,26 @@ static void fitTrack(const TrackIn &in, const std::vector<Plane> &planes,
     TrackState *prev = &states[n - 1];
     for (int i = 0; i < 6; ++i) prev->smth[i] = prev->filt[i];
     prev->smthCov = prev->filtCov;
+    SReal xsPrev[6];
+    M6 csPrev = toM6(prev->smthCov);
+    for (int i = 0; i < 6; ++i) xsPrev[i] = prev->smth[i];
     for (int i = n - 2; i >= 0; --i) {
       TrackState &ts = states[i];
-      Mat<6, 6> G = mul(mul(ts.filtCov, tr(prev->jac)), inverse6(prev->predCov));
-      if (hasNaN(G)) return false;
-      double dp[6];
-      for (int j = 0; j < 6; ++j) dp[j] = prev->smth[j] - prev->pred[j];
+      const M6 cf = toM6(ts.filtCov), cp = toM6(prev->predCov);
+      M6 G = mul6(mul6(cf, tr6(toM6(prev->jac))), inverse6s(cp));
+      if (hasNaN(fromM6(G))) return false;
+      SReal dp[6], xs[6];
+      for (int j = 0; j < 6; ++j) dp[j] = xsPrev[j] - (SReal)prev->pred[j];
       for (int r = 0; r < 6; ++r) {
-        double g = 0.;
+        SReal g = 0;
         for (int j = 0; j < 6; ++j) g += G.a[r][j] * dp[j];
-        ts.smth[r] = ts.filt[r] + g;
+        xs[r] = (SReal)ts.filt[r] + g;
+        ts.smth[r] = (double)xs[r];
       }
-      ts.smthCov =
-          sub(ts.filtCov, mul(mul(G, sub(prev->predCov, prev->smthCov)), tr(G)));
+      const M6 cs = sub6(cf, mul6(mul6(G, sub6(cp, csPrev)), tr6(G)));
+      ts.smthCov = fromM6(cs);
+      for (int r = 0; r < 6; ++r) xsPrev[r] = xs[r];
+      csPrev = cs;
       prev = &ts;
     }
     const TrackState &first = states[0];

@@ -41,9 +41,9 @@ def test_version_and_defaults(kf):
 def test_workspace_size(kf):
     lib = kf.load()
     cfg = kf.default_config()
-    assert lib.kf_workspace_size(C.byref(cfg), 1000, 10) == 10 * 79 * 1000 * 8
+    assert lib.kf_workspace_size(C.byref(cfg), 1000, 10) == 10 * 37 * 1000 * 8
     assert lib.kf_workspace_size(C.byref(cfg), 0, 10) == 0
-    assert lib.kf_host_staging_size(C.byref(cfg), 1000, 10, 0) > 10 * 79 * 1000 * 8
+    assert lib.kf_host_staging_size(C.byref(cfg), 1000, 10, 0) > 10 * 37 * 1000 * 8
 
 
 def test_argument_validation_without_gpu(kf):

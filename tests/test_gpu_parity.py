@@ -2,12 +2,14 @@
 
 Tolerance: 1e-9 relative on fitted parameters (scale max(|x|, sigma_x)),
 covariance elements (scale sqrt(C_ii C_jj)) and chi2 (scale max(chi2, 1));
-status, measurement count and RK step count must be identical.
+status, measurement count, RK step and trial counts must be identical.  The
+comparison point is the oracle's "precise" build (smoother in extended
+precision), see _compare.
 """
 import numpy as np
 import pytest
 
-from conftest import rel_close
+from conftest import parity_report
 
 pytestmark = pytest.mark.gpu
 
@@ -16,14 +18,21 @@ DIAG = [0, 6, 11, 15, 18, 20]
 
 
 def _compare(g, o, tol=TOL):
+    """Identical control flow and 1e-9 relative agreement on every track.
+
+    ``o`` comes from the oracle's "precise" build, which evaluates the
+    reference smoother formula in extended precision (its FP64 evaluation
+    scatters by up to ~2e-8 relative on the q/p variance).
+    """
     assert np.array_equal(g["status"], o["status"]), np.nonzero(g["status"] != o["status"])
     assert np.array_equal(g["n_meas"], o["n_meas"])
     assert np.array_equal(g["n_steps"], o["n_steps"])
     assert np.array_equal(g["n_trials"], o["n_trials"])
     ok = o["status"] == 0
-    worst = rel_close(g, o, tol, mask=ok)
-    assert worst <= 1.0, f"worst relative deviation {worst * tol:.3e} > {tol}"
-    return worst
+    rep = parity_report(g, o, tol, mask=ok)
+    print("gpu vs oracle:", rep)
+    assert rep["params"] <= 1.0 and rep["chi2"] <= 1.0 and rep["cov"] <= 1.0, rep
+    return rep
 
 
 @pytest.mark.parametrize("overstep", [0.01, 0.1])
@@ -34,7 +43,7 @@ def test_config0_parity(kf, orc, overstep):
     tel = kf.make_telescope(1000)
     cfg = kf.default_config(overstep_limit=overstep)
     g = kf.fit_device(tel, cfg)
-    o = orc.fit(tel, cfg, threads=0)
+    o = orc.fit(tel, cfg, threads=0, variant="precise")
     _compare(g, o)
     if overstep == 0.1:
         assert np.all(g["status"] == 0)
@@ -53,7 +62,7 @@ def test_smoothed_states_parity(kf, orc):
     tel = kf.make_telescope(300)
     cfg = kf.default_config(overstep_limit=0.1)
     g = kf.fit_device(tel, cfg, smoothed=True)
-    o = orc.fit(tel, cfg, threads=0, smoothed=True)
+    o = orc.fit(tel, cfg, threads=0, smoothed=True, variant="precise")
     sg, so = g["smoothed"], o["smoothed"]
     for k in range(tel.n_surfaces):
         sig = np.sqrt(so[k, 6 + np.array(DIAG)])
@@ -66,7 +75,7 @@ def test_config1_100k_parity(kf, orc):
     tel = kf.make_telescope(100_000, seed=42)
     cfg = kf.default_config(overstep_limit=0.1)
     g = kf.fit_device(tel, cfg)
-    o = orc.fit(tel, cfg, threads=0)
+    o = orc.fit(tel, cfg, threads=0, variant="precise")
     _compare(g, o)
 
 
@@ -74,27 +83,27 @@ def test_faithful_and_rebuilt_jacobian(kf, orc):
     tel = kf.make_telescope(500, seed=3)
     for faithful in (1, 0):
         cfg = kf.default_config(overstep_limit=0.1, faithful_jacobian=faithful)
-        _compare(kf.fit_device(tel, cfg), orc.fit(tel, cfg, threads=0))
+        _compare(kf.fit_device(tel, cfg), orc.fit(tel, cfg, threads=0, variant="precise"))
 
 
 def test_holes_outliers_parity(kf, orc):
     tel = kf.make_telescope(20_000, n_planes=30, x_first=50., x_step=50., min_len=5, max_len=30,
                            hit_prob=0.9, outlier_prob=0.02, seed=11)
     cfg = kf.default_config(overstep_limit=0.1, outlier_chi2_cut=25.0)
-    _compare(kf.fit_device(tel, cfg), orc.fit(tel, cfg, threads=0))
+    _compare(kf.fit_device(tel, cfg), orc.fit(tel, cfg, threads=0, variant="precise"))
 
 
 def test_field_map_parity(kf, orc):
     tel = kf.make_telescope(3000, n_planes=30, x_first=50., x_step=50., field_map=True, seed=5)
     cfg = kf.default_config(overstep_limit=0.1)
-    _compare(kf.fit_device(tel, cfg), orc.fit(tel, cfg, threads=0))
+    _compare(kf.fit_device(tel, cfg), orc.fit(tel, cfg, threads=0, variant="precise"))
 
 
 def test_edge_cases(kf, orc):
     cfg = kf.default_config(overstep_limit=0.1)
     for n in (1, 31, 33, 129):
         tel = kf.make_telescope(n, seed=n)
-        _compare(kf.fit_device(tel, cfg), orc.fit(tel, cfg, threads=1))
+        _compare(kf.fit_device(tel, cfg), orc.fit(tel, cfg, threads=1, variant="precise"))
     tel = kf.make_telescope(64, seed=9)
     tel.start[4, 0] = 0.0
     tel.start[2, 1] = np.nan
@@ -102,7 +111,7 @@ def test_edge_cases(kf, orc):
     tel.hit_mask[3] = 1          # a single hit
     tel.n_planes[4] = 1
     g = kf.fit_device(tel, cfg)
-    o = orc.fit(tel, cfg, threads=1)
+    o = orc.fit(tel, cfg, threads=1, variant="precise")
     assert g["status"][0] == 5 and g["status"][1] == 5 and g["status"][2] == 4
     _compare(g, o)
 

@@ -182,3 +182,20 @@ def test_bad_inputs_and_no_hits(kf, orc):
     o = orc.fit(tel, kf.default_config(overstep_limit=0.1), threads=1)
     assert o["status"][0] == 5 and o["status"][1] == 5 and o["status"][2] == 4
     assert np.all(o["status"][3:] == 0)
+
+
+def test_reference_smoother_fp64_scatter(kf, orc):
+    """The reference smoother's covariance update C_f - G (C_p' - C_s') G^T
+    cancels heavily for the q/p variance: its FP64 evaluation scatters by
+    up to ~1e-8 relative around the extended-precision value, while the
+    parameters, chi2 and the control flow are unaffected."""
+    from conftest import parity_report
+    tel = kf.make_telescope(3000, n_planes=30, x_first=50., x_step=50., field_map=True, seed=5)
+    cfg = kf.default_config(overstep_limit=0.1)
+    d = orc.fit(tel, cfg, threads=0)
+    p = orc.fit(tel, cfg, threads=0, variant="precise")
+    for k in ("status", "n_meas", "n_steps", "n_trials"):
+        assert np.array_equal(d[k], p[k])
+    rep = parity_report(d, p, 1e-9)
+    assert rep["params"] <= 1.0 and rep["chi2"] <= 1.0
+    assert 1.0 < rep["cov"] < 100.0, rep
