@@ -20,7 +20,7 @@ import numpy as np
 RK_TRIAL = 94      # one tryRungeKuttaStep: 2 field points, k1..k4, error estimate
 RK_STEP = 591      # accepted step: time, transport matrix blocks, D*J on 25 entries, motion
 FILTER = 950       # boundState to a plane (J C J^T on the non-zeros) + gain update + reload
-SMOOTH = 1726      # one RTS smoother state: LDL^T inverse, gain, state and covariance
+SMOOTH = 652       # one RTS smoother state: structured J^-1 (gain), state, G C G^T
 FIXED = 800        # start state on the perigee line, final transport to the line
 
 # dense reference formulation, same events
