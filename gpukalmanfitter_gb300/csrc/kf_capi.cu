@@ -10,9 +10,14 @@
 #include <cstdio>
 #include <cstring>
 
-#include "kf_device.cuh"
+#include "kf_kernels.cuh"
 
 using namespace kfd;
+
+// defined in kf_fit_fp64.cu / kf_fit_mixed.cu (one instantiation each, so the
+// two compile in parallel)
+cudaError_t launchFitFp64(const kfd::Params &P, unsigned grid, cudaStream_t s);
+cudaError_t launchFitMixed(const kfd::Params &P, unsigned grid, cudaStream_t s);
 
 namespace {
 
@@ -26,39 +31,6 @@ int32_t fail(int32_t code, const char *fmt, const char *detail = "") {
 int32_t cudaFail(cudaError_t e, const char *where) {
   std::snprintf(g_err, sizeof(g_err), "%s: %s", where, cudaGetErrorString(e));
   return KF_ERR_CUDA;
-}
-
-// Warp-synchronous driver: lanes step independently and park at heavy actor
-// work (filter update, smoothing, final transport); when every lane of the
-// warp is parked or done the parked lanes run their events together, so the
-// FP64-heavy Kalman algebra executes without divergence.
-template <int BS>
-__global__ void __launch_bounds__(BS) fitFp64Kernel(const __grid_constant__ Params P) {
-  __shared__ PlaneD sp[KF_MAX_PLANES];
-  for (int k = threadIdx.x; k < P.nSurf; k += BS) sp[k] = P.planes[k];
-  __syncthreads();
-  const int64_t i = (int64_t)blockIdx.x * BS + threadIdx.x;
-  Lane L;
-  initLane(L, P, sp, i);
-  for (;;) {
-    if (!L.parked && L.pc != PC_DONE) advance(L, P, sp);
-    const bool waiting = L.parked || L.pc == PC_DONE;
-    if (__all_sync(0xffffffffu, waiting)) {
-      if (L.parked) runEvent(L, P, sp);
-      if (__all_sync(0xffffffffu, L.pc == PC_DONE)) break;
-    }
-  }
-  if (i < P.n) {
-    P.oStatus[i] = L.status;
-    P.oChi2[i] = L.chi2;
-    P.oNMeas[i] = L.measStates;
-    if (P.oNSteps) P.oNSteps[i] = L.rkSteps;
-    if (P.oNTrials) P.oNTrials[i] = L.rkTrials;
-    if (L.status != KF_TRACK_OK && !L.finished) {
-      for (int e = 0; e < 6; ++e) P.oParams[(size_t)e * P.stride + i] = 0.;
-      for (int e = 0; e < 21; ++e) P.oCov[(size_t)e * P.stride + i] = 0.;
-    }
-  }
 }
 
 size_t wsBytes(int64_t n, int32_t nSurf) {
@@ -78,8 +50,8 @@ int32_t checkCommon(const kf_inputs_t *in, const kf_config_t *cfg, const kf_geom
   if (field->kind == KF_FIELD_GRID3D &&
       (!field->grid || field->nx < 2 || field->ny < 2 || field->nz < 2))
     return fail(KF_ERR_INVALID_ARGUMENT, "bad field grid%s");
-  if (cfg->precision != KF_PRECISION_FP64)
-    return fail(KF_ERR_UNSUPPORTED, "precision mode not available%s");
+  if (cfg->precision != KF_PRECISION_FP64 && cfg->precision != KF_PRECISION_MIXED)
+    return fail(KF_ERR_UNSUPPORTED, "unknown precision mode%s");
   if (cfg->max_steps < 0 || cfg->max_rk_trials < 0)
     return fail(KF_ERR_INVALID_ARGUMENT, "negative step limits%s");
   return KF_SUCCESS;
@@ -145,13 +117,13 @@ void fillParams(Params &P, const kf_inputs_t *in, const kf_outputs_t *out, const
   }
 }
 
-int32_t launchFit(const Params &P, int blockSize, cudaStream_t s) {
+int32_t launchFit(const Params &P, int precision, int blockSize, cudaStream_t s) {
   (void)blockSize;
   if (P.n == 0) return KF_SUCCESS;
-  constexpr int bs = 128;
-  const unsigned grid = (unsigned)((P.n + bs - 1) / bs);
-  fitFp64Kernel<bs><<<grid, bs, 0, s>>>(P);
-  cudaError_t e = cudaGetLastError();
+  const unsigned grid = (unsigned)((P.n + kFitBlock - 1) / kFitBlock);
+  cudaError_t e = (precision == KF_PRECISION_MIXED) ? launchFitMixed(P, grid, s)
+                                                    : launchFitFp64(P, grid, s);
+  if (e == cudaSuccess) e = cudaGetLastError();
   if (e != cudaSuccess) return cudaFail(e, "fit kernel launch");
   return KF_SUCCESS;
 }
@@ -201,7 +173,7 @@ int32_t kf_fit_batch(const kf_inputs_t *in, kf_outputs_t *out, const kf_config_t
     return fail(KF_ERR_WORKSPACE_TOO_SMALL, "workspace smaller than kf_workspace_size()%s");
   Params P;
   fillParams(P, in, out, cfg, geo, field, workspace);
-  return launchFit(P, cfg->block_size, static_cast<cudaStream_t>(stream));
+  return launchFit(P, cfg->precision, cfg->block_size, static_cast<cudaStream_t>(stream));
 }
 
 // ---- host-buffer convenience ----------------------------------------------

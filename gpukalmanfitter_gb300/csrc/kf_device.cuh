@@ -21,6 +21,15 @@
 // multiplication, and the bound-to-bound Jacobian has a zero last column
 // except J(5,5) = 1 and a unit row 4.  Skipped terms are exact zeros and ones,
 // so the result is the reference's algebra with a different rounding order.
+//
+// Precision.  Lane<R> carries the transport Jacobians in R.  R = double is
+// the plain form (FP64 throughout).  R = float is the mixed form: field
+// interpolation, RK4 stages, the error estimate, the transport matrix and all
+// Jacobians in FP32; position, direction, time, step sizes, covariance, gain
+// (Joseph-form update) and smoother in FP64.  The mixed form accepts or
+// rejects an RK trial on its FP32 error estimate unless that estimate lies
+// within 1 % of the tolerance, where the trial is re-evaluated in FP64, so
+// its step sequence follows the FP64 fit's.
 #pragma once
 
 #include <cfloat>
@@ -72,9 +81,25 @@ __host__ __device__ constexpr int ut(int i, int j) {
 }
 __device__ __forceinline__ int sidx(int i, int j) { return i <= j ? ut(i, j) : ut(j, i); }
 
+template <typename T>
+__device__ __forceinline__ void cross3(const T a[3], const T b[3], T r[3]) {
+  r[0] = a[1] * b[2] - a[2] * b[1];
+  r[1] = a[2] * b[0] - a[0] * b[2];
+  r[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+// std::max / std::min argument semantics (NaN handling as in the reference)
+__device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }
+__device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }
+
+enum { kAccuracy = 0, kActor = 1, kAborter = 2, kUser = 3 };
+enum { kMissed = 0, kReachable = 1, kOnSurface = 2 };
+enum { PC_PRE = 0, PC_LOOP = 1, PC_ACT = 2, PC_POST = 3, PC_DONE = 4 };
+
 // ---------------------------------------------------------------------------
 // Magnetic field lookup: Test::ConstantBField (Test/Helper.hpp:17-22) or the
-// trilinear map (MagneticField/InterpolatedBFieldMap.hpp:178-181).
+// trilinear map (MagneticField/InterpolatedBFieldMap.hpp:178-181), in FP64
+// (plain form) or FP32 (mixed form).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void getField(const FieldD &F, const double p[3], double B[3]) {
   if (F.kind == KF_FIELD_CONSTANT) {
@@ -115,21 +140,49 @@ __device__ __forceinline__ void getField(const FieldD &F, const double p[3], dou
   B[2] = tri(v000.z, v100.z, v010.z, v110.z, v001.z, v101.z, v011.z, v111.z);
 }
 
-__device__ __forceinline__ void cross3(const double a[3], const double b[3], double r[3]) {
-  r[0] = a[1] * b[2] - a[2] * b[1];
-  r[1] = a[2] * b[0] - a[0] * b[2];
-  r[2] = a[0] * b[1] - a[1] * b[0];
+__device__ __forceinline__ void getField(const FieldD &F, const float p[3], float B[3]) {
+  if (F.kind == KF_FIELD_CONSTANT) {
+    B[0] = (float)F.B[0];
+    B[1] = (float)F.B[1];
+    B[2] = (float)F.B[2];
+    return;
+  }
+  int idx[3];
+  float f[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    float g = (p[a] - (float)F.mn[a]) * (float)F.invw[a];
+    int i = (int)floorf(g);
+    i = min(max(i, 0), F.n[a] - 2);
+    idx[a] = i;
+    f[a] = g - (float)i;
+  }
+  const size_t nx = F.n[0], nxy = (size_t)F.n[0] * F.n[1];
+  const size_t base = (size_t)idx[2] * nxy + (size_t)idx[1] * nx + idx[0];
+  const float4 v000 = __ldg(F.grid + base), v100 = __ldg(F.grid + base + 1);
+  const float4 v010 = __ldg(F.grid + base + nx), v110 = __ldg(F.grid + base + nx + 1);
+  const float4 v001 = __ldg(F.grid + base + nxy), v101 = __ldg(F.grid + base + nxy + 1);
+  const float4 v011 = __ldg(F.grid + base + nxy + nx), v111 = __ldg(F.grid + base + nxy + nx + 1);
+  const float sc = (float)F.scale;
+  auto tri = [&](float a000, float a100, float a010, float a110, float a001, float a101,
+                 float a011, float a111) {
+    float c00 = a000 + f[0] * (a100 - a000);
+    float c10 = a010 + f[0] * (a110 - a010);
+    float c01 = a001 + f[0] * (a101 - a001);
+    float c11 = a011 + f[0] * (a111 - a011);
+    float c0 = c00 + f[1] * (c10 - c00);
+    float c1 = c01 + f[1] * (c11 - c01);
+    return (c0 + f[2] * (c1 - c0)) * sc;
+  };
+  B[0] = tri(v000.x, v100.x, v010.x, v110.x, v001.x, v101.x, v011.x, v111.x);
+  B[1] = tri(v000.y, v100.y, v010.y, v110.y, v001.y, v101.y, v011.y, v111.y);
+  B[2] = tri(v000.z, v100.z, v010.z, v110.z, v001.z, v101.z, v011.z, v111.z);
 }
 
-// std::max / std::min argument semantics (NaN handling as in the reference)
-__device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }
-__device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }
-
-enum { kAccuracy = 0, kActor = 1, kAborter = 2, kUser = 3 };
-enum { kMissed = 0, kReachable = 1, kOnSurface = 2 };
-enum { PC_PRE = 0, PC_LOOP = 1, PC_ACT = 2, PC_POST = 3, PC_DONE = 4 };
-
-struct Lane {
+// ---------------------------------------------------------------------------
+// Per-track state
+// ---------------------------------------------------------------------------
+template <typename R> struct Lane {
   // ---- stepper state (EigenStepper::State)
   double pos[3], dir[3];
   double p, q, t;
@@ -137,10 +190,10 @@ struct Lane {
   double ss[4]; // ConstrainedStep values
   int ssDir;    // ConstrainedStep direction (+1 / -1)
   int navDir;
-  double JA[3][3], Ja[3], Jb, JB[3][3], Jc[3]; // transport Jacobian blocks
-  double G03[3][4]; // jacToGlobal rows 0-2, cols 0-3
-  double G46[3][2]; // jacToGlobal rows 4-6, cols 2-3
-  double der[7];    // derivative rows 0..6 (row 7 is always 0)
+  R JA[3][3], Ja[3], Jb, JB[3][3], Jc[3]; // transport Jacobian blocks
+  R G03[3][4]; // jacToGlobal rows 0-2, cols 0-3
+  R G46[3][2]; // jacToGlobal rows 4-6, cols 2-3
+  R der[7];    // derivative rows 0..6 (row 7 is always 0)
   double cov[21];
   // per-leg constants (functions of p only)
   double qop, dtds, d37;
@@ -155,31 +208,55 @@ struct Lane {
   int64_t idx;
 };
 
-// ---- ConstrainedStep -------------------------------------------------------
-__device__ __forceinline__ double ssMax(const Lane &L) {
-  double m = -DBL_MAX;
+// ---- ConstrainedStep (ConstrainedStep.hpp:22-108) --------------------------
+// min/max/abs comparisons run on an order-preserving integer image of the
+// doubles (integer pipe), selecting exactly the values the double comparisons
+// select for non-NaN operands.
+__device__ __forceinline__ long long okey(double x) {
+  const long long b = __double_as_longlong(x);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ long long akey(double x) {
+  return __double_as_longlong(x) & 0x7fffffffffffffffLL;
+}
+template <typename R> __device__ __forceinline__ double ssMax(const Lane<R> &L) {
+  double m = L.ss[0];
+  long long km = okey(m);
 #pragma unroll
-  for (int i = 0; i < 4; ++i) m = (L.ss[i] > m) ? L.ss[i] : m;
+  for (int i = 1; i < 4; ++i) {
+    const long long k = okey(L.ss[i]);
+    if (k > km) {
+      km = k;
+      m = L.ss[i];
+    }
+  }
   return m;
 }
-__device__ __forceinline__ double ssMin(const Lane &L) {
-  double m = DBL_MAX;
+template <typename R> __device__ __forceinline__ double ssMin(const Lane<R> &L) {
+  double m = L.ss[0];
+  long long km = okey(m);
 #pragma unroll
-  for (int i = 0; i < 4; ++i) m = (L.ss[i] < m) ? L.ss[i] : m;
+  for (int i = 1; i < 4; ++i) {
+    const long long k = okey(L.ss[i]);
+    if (k < km) {
+      km = k;
+      m = L.ss[i];
+    }
+  }
   return m;
 }
-__device__ __forceinline__ double ssValue(const Lane &L) {
+template <typename R> __device__ __forceinline__ double ssValue(const Lane<R> &L) {
   return L.ssDir == 1 ? ssMin(L) : ssMax(L);
 }
-__device__ __forceinline__ void ssRelease(Lane &L, int t) {
+template <typename R> __device__ __forceinline__ void ssRelease(Lane<R> &L, int t) {
   L.ss[t] = (L.ssDir == 1) ? ssMax(L) : ssMin(L);
 }
-__device__ __forceinline__ void ssUpdate(Lane &L, double v, int t, bool rel) {
+template <typename R> __device__ __forceinline__ void ssUpdate(Lane<R> &L, double v, int t, bool rel) {
   if (rel) ssRelease(L, t);
   const double c = L.ss[t];
-  L.ss[t] = fabs(c) < fabs(v) ? c : v;
+  L.ss[t] = akey(c) < akey(v) ? c : v;
 }
-__device__ __forceinline__ void ssInit(Lane &L, double value) {
+template <typename R> __device__ __forceinline__ void ssInit(Lane<R> &L, double value) {
   L.ssDir = value > 0. ? 1 : -1;
   L.ss[0] = DBL_MAX * L.ssDir;
   L.ss[1] = DBL_MAX * L.ssDir;
@@ -188,47 +265,47 @@ __device__ __forceinline__ void ssInit(Lane &L, double value) {
 }
 
 // per-leg constants: q/p, dt/ds and the dt/d(q/p) coefficient
-__device__ __forceinline__ void legConstants(Lane &L, double mass) {
+template <typename R> __device__ __forceinline__ void legConstants(Lane<R> &L, double mass) {
   L.qop = L.q / L.p;
   L.dtds = hypot(1., mass / L.p);
   L.d37 = mass * mass * L.q / (L.p * L.dtds);
 }
 
 // ---- Jacobian resets -------------------------------------------------------
-__device__ __forceinline__ void resetTransport(Lane &L) {
+template <typename R> __device__ __forceinline__ void resetTransport(Lane<R> &L) {
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-      L.JA[i][j] = 0.;
-      L.JB[i][j] = (i == j) ? 1. : 0.;
+      L.JA[i][j] = R(0);
+      L.JB[i][j] = (i == j) ? R(1) : R(0);
     }
-    L.Ja[i] = 0.;
-    L.Jc[i] = 0.;
+    L.Ja[i] = R(0);
+    L.Jc[i] = R(0);
   }
-  L.Jb = 0.;
+  L.Jb = R(0);
 #pragma unroll
-  for (int i = 0; i < 7; ++i) L.der[i] = 0.;
+  for (int i = 0; i < 7; ++i) L.der[i] = R(0);
 }
 
 // PlaneSurface::initJacobianToGlobal (PlaneSurface.ipp:122-156)
-__device__ __forceinline__ void planeJacToGlobal(Lane &L, const PlaneD &pl) {
-  const double x = L.dir[0], y = L.dir[1], z = L.dir[2];
-  const double cosT = z, sinT = sqrt(x * x + y * y);
-  const double inv = 1. / sinT;
-  const double cosP = x * inv, sinP = y * inv;
+template <typename R> __device__ __forceinline__ void planeJacToGlobal(Lane<R> &L, const PlaneD &pl) {
+  const R x = (R)L.dir[0], y = (R)L.dir[1], z = (R)L.dir[2];
+  const R cosT = z, sinT = sqrt(x * x + y * y);
+  const R inv = R(1) / sinT;
+  const R cosP = x * inv, sinP = y * inv;
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
-    L.G03[r][0] = pl.U[r];
-    L.G03[r][1] = pl.V[r];
-    L.G03[r][2] = 0.;
-    L.G03[r][3] = 0.;
+    L.G03[r][0] = (R)pl.U[r];
+    L.G03[r][1] = (R)pl.V[r];
+    L.G03[r][2] = R(0);
+    L.G03[r][3] = R(0);
   }
   L.G46[0][0] = (-sinT) * sinP;
   L.G46[0][1] = cosT * cosP;
   L.G46[1][0] = sinT * cosP;
   L.G46[1][1] = cosT * sinP;
-  L.G46[2][0] = 0.;
+  L.G46[2][0] = R(0);
   L.G46[2][1] = (-sinT);
 }
 
@@ -250,177 +327,255 @@ __device__ __forceinline__ void lineFrame(const double mom[3], double X[3], doub
 // ---------------------------------------------------------------------------
 // EigenStepper::step (EigenStepper.ipp:226-332)
 // ---------------------------------------------------------------------------
-__device__ void rkStep(Lane &L, const Params &P) {
-  double Bf[3], Bm[3], Bl[3], k1[3], k2[3], k3[3], k4[3];
-  double err = 0.;
-  const double qop = L.qop;
-  getField(P.field, L.pos, Bf);
-  {
-    double c[3];
-    cross3(L.dir, Bf, c);
-    k1[0] = qop * c[0];
-    k1[1] = qop * c[1];
-    k1[2] = qop * c[2];
-  }
-  long nTrials = 0;
-  double h = ssValue(L);
-  for (;;) {
-    L.rkTrials++;
-    // tryRungeKuttaStep
-    const double h2 = h * h, half_h = h * 0.5;
-    double pos1[3], tmp[3], c[3];
+template <typename T> struct RkStages {
+  T Bf[3], Bm[3], Bl[3], k1[3], k2[3], k3[3], k4[3];
+};
+
+// k1 at the current point (evaluatek, EigenStepper.ipp:18-33)
+template <typename T>
+__device__ __forceinline__ void rkFirst(const FieldD &F, const T pos[3], const T dir[3], T qop,
+                                        RkStages<T> &s) {
+  getField(F, pos, s.Bf);
+  T c[3];
+  cross3(dir, s.Bf, c);
 #pragma unroll
-    for (int i = 0; i < 3; ++i) pos1[i] = L.pos[i] + half_h * L.dir[i] + (h2 * 0.125) * k1[i];
-    getField(P.field, pos1, Bm);
+  for (int i = 0; i < 3; ++i) s.k1[i] = qop * c[i];
+}
+
+// tryRungeKuttaStep (EigenStepper.ipp:243-269): k2, k3, k4 and the error
+// estimate h^2 |k1 - k2 - k3 + k4|_1
+template <typename T>
+__device__ __forceinline__ T rkTrial(const FieldD &F, const T pos[3], const T dir[3], T qop, T h,
+                                     RkStages<T> &s) {
+  const T h2 = h * h, half_h = h * T(0.5);
+  T pos1[3], tmp[3], c[3];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) tmp[i] = L.dir[i] + half_h * k1[i];
-    cross3(tmp, Bm, c);
+  for (int i = 0; i < 3; ++i) pos1[i] = pos[i] + half_h * dir[i] + (h2 * T(0.125)) * s.k1[i];
+  getField(F, pos1, s.Bm);
 #pragma unroll
-    for (int i = 0; i < 3; ++i) k2[i] = qop * c[i];
+  for (int i = 0; i < 3; ++i) tmp[i] = dir[i] + half_h * s.k1[i];
+  cross3(tmp, s.Bm, c);
 #pragma unroll
-    for (int i = 0; i < 3; ++i) tmp[i] = L.dir[i] + half_h * k2[i];
-    cross3(tmp, Bm, c);
+  for (int i = 0; i < 3; ++i) s.k2[i] = qop * c[i];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) k3[i] = qop * c[i];
-    double pos2[3];
+  for (int i = 0; i < 3; ++i) tmp[i] = dir[i] + half_h * s.k2[i];
+  cross3(tmp, s.Bm, c);
 #pragma unroll
-    for (int i = 0; i < 3; ++i) pos2[i] = L.pos[i] + h * L.dir[i] + (h2 * 0.5) * k3[i];
-    getField(P.field, pos2, Bl);
+  for (int i = 0; i < 3; ++i) s.k3[i] = qop * c[i];
+  T pos2[3];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) tmp[i] = L.dir[i] + h * k3[i];
-    cross3(tmp, Bl, c);
+  for (int i = 0; i < 3; ++i) pos2[i] = pos[i] + h * dir[i] + (h2 * T(0.5)) * s.k3[i];
+  getField(F, pos2, s.Bl);
 #pragma unroll
-    for (int i = 0; i < 3; ++i) k4[i] = qop * c[i];
-    const double d0 = k1[0] - k2[0] - k3[0] + k4[0];
-    const double d1 = k1[1] - k2[1] - k3[1] + k4[1];
-    const double d2 = k1[2] - k2[2] - k3[2] + k4[2];
-    err = smax(h2 * (fabs(d0) + fabs(d1) + fabs(d2)), 1e-20);
-    if (err <= P.tol) break;
-    const double scale = smin(smax(0.25, pow(P.tol / fabs(2. * err), 0.25)), 4.);
-    const double hn = h * scale;
-    L.ss[kAccuracy] = hn;
-    L.ssDir = hn > 0. ? 1 : -1;
-    h = ssValue(L);
-    if (h * h < P.cutoff * P.cutoff) return;
-    if (nTrials > P.maxTrials) return;
-    nTrials++;
-  }
-  // propagationTime (EigenStepper.ipp:36-47)
-  L.t += h * L.dtds;
-  L.der[3] = L.dtds;
-  // transportMatrix (EigenStepper.ipp:50-124) on its non-zero blocks, and
-  // jacTransport = D * jacTransport
-  {
-    const double half_h = h * 0.5;
-    double dk1dL[3], dk2dL[3], dk3dL[3], dk4dL[3], tmp[3], c[3], cc[3];
-    cross3(L.dir, Bf, dk1dL);
+  for (int i = 0; i < 3; ++i) tmp[i] = dir[i] + h * s.k3[i];
+  cross3(tmp, s.Bl, c);
 #pragma unroll
-    for (int i = 0; i < 3; ++i) tmp[i] = L.dir[i] + half_h * k1[i];
-    cross3(tmp, Bm, c);
-    cross3(dk1dL, Bm, cc);
+  for (int i = 0; i < 3; ++i) s.k4[i] = qop * c[i];
+  const T d0 = s.k1[0] - s.k2[0] - s.k3[0] + s.k4[0];
+  const T d1 = s.k1[1] - s.k2[1] - s.k3[1] + s.k4[1];
+  const T d2 = s.k1[2] - s.k2[2] - s.k3[2] + s.k4[2];
+  const T e = h2 * (fabs(d0) + fabs(d1) + fabs(d2));
+  return (e < T(1e-20)) ? T(1e-20) : e;
+}
+
+// transportMatrix (EigenStepper.ipp:50-124) on its non-zero blocks and
+// jacTransport = D * jacTransport (EigenStepper.ipp:312-318)
+template <typename R>
+__device__ __forceinline__ void transportUpdate(Lane<R> &L, const R dir[3], R qop, R h, R d37,
+                                                const RkStages<R> &s) {
+  const R half_h = h * R(0.5);
+  R dk1dL[3], dk2dL[3], dk3dL[3], dk4dL[3], tmp[3], c[3], cc[3];
+  cross3(dir, s.Bf, dk1dL);
 #pragma unroll
-    for (int i = 0; i < 3; ++i) dk2dL[i] = c[i] + (qop * half_h) * cc[i];
+  for (int i = 0; i < 3; ++i) tmp[i] = dir[i] + half_h * s.k1[i];
+  cross3(tmp, s.Bm, c);
+  cross3(dk1dL, s.Bm, cc);
 #pragma unroll
-    for (int i = 0; i < 3; ++i) tmp[i] = L.dir[i] + half_h * k2[i];
-    cross3(tmp, Bm, c);
-    cross3(dk2dL, Bm, cc);
+  for (int i = 0; i < 3; ++i) dk2dL[i] = c[i] + (qop * half_h) * cc[i];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) dk3dL[i] = c[i] + (qop * half_h) * cc[i];
+  for (int i = 0; i < 3; ++i) tmp[i] = dir[i] + half_h * s.k2[i];
+  cross3(tmp, s.Bm, c);
+  cross3(dk2dL, s.Bm, cc);
 #pragma unroll
-    for (int i = 0; i < 3; ++i) tmp[i] = L.dir[i] + h * k3[i];
-    cross3(tmp, Bl, c);
-    cross3(dk3dL, Bl, cc);
+  for (int i = 0; i < 3; ++i) dk3dL[i] = c[i] + (qop * half_h) * cc[i];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) dk4dL[i] = c[i] + (qop * h) * cc[i];
-    // dk1dT = qop * [B]x
-    double T1[3][3];
-    T1[0][0] = 0.;
-    T1[0][1] = qop * Bf[2];
-    T1[0][2] = qop * -Bf[1];
-    T1[1][0] = qop * -Bf[2];
-    T1[1][1] = 0.;
-    T1[1][2] = qop * Bf[0];
-    T1[2][0] = qop * Bf[1];
-    T1[2][1] = qop * -Bf[0];
-    T1[2][2] = 0.;
-    // dk(n+1)dT = qop * colcross(I + hh * dkndT, B)
-    double T2[3][3], T3[3][3], T4[3][3];
-    auto nextT = [&](const double (&Tp)[3][3], double hh, const double Bx[3],
-                     double (&To)[3][3]) {
+  for (int i = 0; i < 3; ++i) tmp[i] = dir[i] + h * s.k3[i];
+  cross3(tmp, s.Bl, c);
+  cross3(dk3dL, s.Bl, cc);
 #pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        double col[3], r[3];
+  for (int i = 0; i < 3; ++i) dk4dL[i] = c[i] + (qop * h) * cc[i];
+  // dk1dT = qop * [B]x
+  R T1[3][3];
+  T1[0][0] = R(0);
+  T1[0][1] = qop * s.Bf[2];
+  T1[0][2] = qop * -s.Bf[1];
+  T1[1][0] = qop * -s.Bf[2];
+  T1[1][1] = R(0);
+  T1[1][2] = qop * s.Bf[0];
+  T1[2][0] = qop * s.Bf[1];
+  T1[2][1] = qop * -s.Bf[0];
+  T1[2][2] = R(0);
+  // dk(n+1)dT = qop * colcross(I + hh * dkndT, B)
+  R T2[3][3], T3[3][3], T4[3][3];
+  auto nextT = [&](const R (&Tp)[3][3], R hh, const R Bx[3], R (&To)[3][3]) {
 #pragma unroll
-        for (int i = 0; i < 3; ++i) col[i] = ((i == j) ? 1. : 0.) + hh * Tp[i][j];
-        cross3(col, Bx, r);
+    for (int j = 0; j < 3; ++j) {
+      R col[3], r[3];
 #pragma unroll
-        for (int i = 0; i < 3; ++i) To[i][j] = qop * r[i];
-      }
-    };
-    nextT(T1, half_h, Bm, T2);
-    nextT(T2, half_h, Bm, T3);
-    nextT(T3, h, Bl, T4);
-    // D blocks: dFdT (A), dGdT (I + Bd), dFdL (a), dGdL (c), D(3,7)
-    double DA[3][3], DB[3][3], Da[3], Dc[3];
-    const double h6 = h / 6.;
+      for (int i = 0; i < 3; ++i) col[i] = ((i == j) ? R(1) : R(0)) + hh * Tp[i][j];
+      cross3(col, Bx, r);
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
-#pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        double v = ((i == j) ? 1. : 0.) + h6 * (T1[i][j] + T2[i][j] + T3[i][j]);
-        DA[i][j] = v * h;
-        DB[i][j] = ((i == j) ? 1. : 0.) + h6 * (T1[i][j] + 2. * (T2[i][j] + T3[i][j]) + T4[i][j]);
-      }
-      Da[i] = (h * h) / 6. * (dk1dL[i] + dk2dL[i] + dk3dL[i]);
-      Dc[i] = h6 * (dk1dL[i] + 2. * (dk2dL[i] + dk3dL[i]) + dk4dL[i]);
+      for (int i = 0; i < 3; ++i) To[i][j] = qop * r[i];
     }
-    const double D37 = h * L.d37;
-    // new J = D * J:
-    //  A' = A + DA*B,  a' = a + DA*c + Da,  b' = b + D37,
-    //  B' = DB*B,      c' = DB*c + Dc
-    double nA[3][3], na[3], nB[3][3], nc[3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-#pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        nA[i][j] = L.JA[i][j] + DA[i][0] * L.JB[0][j] + DA[i][1] * L.JB[1][j] + DA[i][2] * L.JB[2][j];
-        nB[i][j] = DB[i][0] * L.JB[0][j] + DB[i][1] * L.JB[1][j] + DB[i][2] * L.JB[2][j];
-      }
-      na[i] = L.Ja[i] + DA[i][0] * L.Jc[0] + DA[i][1] * L.Jc[1] + DA[i][2] * L.Jc[2] + Da[i];
-      nc[i] = DB[i][0] * L.Jc[0] + DB[i][1] * L.Jc[1] + DB[i][2] * L.Jc[2] + Dc[i];
-    }
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-#pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        L.JA[i][j] = nA[i][j];
-        L.JB[i][j] = nB[i][j];
-      }
-      L.Ja[i] = na[i];
-      L.Jc[i] = nc[i];
-    }
-    L.Jb = L.Jb + D37;
-  }
-  // equations of motion
-  const double hh6 = h * h / 6., h6 = h / 6.;
+  };
+  nextT(T1, half_h, s.Bm, T2);
+  nextT(T2, half_h, s.Bm, T3);
+  nextT(T3, h, s.Bl, T4);
+  // D blocks: dFdT (A), dGdT (I + Bd), dFdL (a), dGdL (c), D(3,7)
+  R DA[3][3], DB[3][3], Da[3], Dc[3];
+  const R h6 = h / R(6);
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    L.pos[i] = L.pos[i] + (h * L.dir[i] + hh6 * (k1[i] + k2[i] + k3[i]));
-    L.dir[i] = L.dir[i] + h6 * (k1[i] + 2. * (k2[i] + k3[i]) + k4[i]);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      R v = ((i == j) ? R(1) : R(0)) + h6 * (T1[i][j] + T2[i][j] + T3[i][j]);
+      DA[i][j] = v * h;
+      DB[i][j] = ((i == j) ? R(1) : R(0)) + h6 * (T1[i][j] + R(2) * (T2[i][j] + T3[i][j]) + T4[i][j]);
+    }
+    Da[i] = (h * h) / R(6) * (dk1dL[i] + dk2dL[i] + dk3dL[i]);
+    Dc[i] = h6 * (dk1dL[i] + R(2) * (dk2dL[i] + dk3dL[i]) + dk4dL[i]);
   }
-  {
+  const R D37 = h * d37;
+  // new J = D * J:
+  //  A' = A + DA*B,  a' = a + DA*c + Da,  b' = b + D37,
+  //  B' = DB*B,      c' = DB*c + Dc
+  R nA[3][3], na[3], nB[3][3], nc[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      nA[i][j] = L.JA[i][j] + DA[i][0] * L.JB[0][j] + DA[i][1] * L.JB[1][j] + DA[i][2] * L.JB[2][j];
+      nB[i][j] = DB[i][0] * L.JB[0][j] + DB[i][1] * L.JB[1][j] + DB[i][2] * L.JB[2][j];
+    }
+    na[i] = L.Ja[i] + DA[i][0] * L.Jc[0] + DA[i][1] * L.Jc[1] + DA[i][2] * L.Jc[2] + Da[i];
+    nc[i] = DB[i][0] * L.Jc[0] + DB[i][1] * L.Jc[1] + DB[i][2] * L.Jc[2] + Dc[i];
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      L.JA[i][j] = nA[i][j];
+      L.JB[i][j] = nB[i][j];
+    }
+    L.Ja[i] = na[i];
+    L.Jc[i] = nc[i];
+  }
+  L.Jb = L.Jb + D37;
+}
+
+template <typename R> __device__ void rkStep(Lane<R> &L, const Params &P) {
+  long nTrials = 0;
+  double h = ssValue(L);
+  if constexpr (sizeof(R) == sizeof(double)) {
+    // ---- plain form: FP64 throughout
+    RkStages<double> s;
+    rkFirst<double>(P.field, L.pos, L.dir, L.qop, s);
+    for (;;) {
+      L.rkTrials++;
+      const double err = rkTrial<double>(P.field, L.pos, L.dir, L.qop, h, s);
+      if (err <= P.tol) break;
+      const double scale = smin(smax(0.25, pow(P.tol / fabs(2. * err), 0.25)), 4.);
+      const double hn = h * scale;
+      L.ss[kAccuracy] = hn;
+      L.ssDir = hn > 0. ? 1 : -1;
+      h = ssValue(L);
+      if (h * h < P.cutoff * P.cutoff) return;
+      if (nTrials > P.maxTrials) return;
+      nTrials++;
+    }
+    // propagationTime (EigenStepper.ipp:36-47)
+    L.t += h * L.dtds;
+    L.der[3] = L.dtds;
+    transportUpdate<double>(L, L.dir, L.qop, h, L.d37, s);
+    // equations of motion
+    const double hh6 = h * h / 6., h6 = h / 6.;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      L.pos[i] = L.pos[i] + (h * L.dir[i] + hh6 * (s.k1[i] + s.k2[i] + s.k3[i]));
+      L.dir[i] = L.dir[i] + h6 * (s.k1[i] + 2. * (s.k2[i] + s.k3[i]) + s.k4[i]);
+    }
     const double n = sqrt(L.dir[0] * L.dir[0] + L.dir[1] * L.dir[1] + L.dir[2] * L.dir[2]);
     const double inv = 1. / n;
     L.dir[0] *= inv;
     L.dir[1] *= inv;
     L.dir[2] *= inv;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      L.der[i] = L.dir[i];
+      L.der[4 + i] = s.k4[i];
+    }
+  } else {
+    // ---- mixed form: FP32 stages, transport and error estimate
+    const float qopf = (float)L.qop;
+    const float posf[3] = {(float)L.pos[0], (float)L.pos[1], (float)L.pos[2]};
+    const float dirf[3] = {(float)L.dir[0], (float)L.dir[1], (float)L.dir[2]};
+    const float tolLo = (float)(P.tol * 0.99), tolHi = (float)(P.tol * 1.01);
+    RkStages<float> s;
+    rkFirst<float>(P.field, posf, dirf, qopf, s);
+    for (;;) {
+      L.rkTrials++;
+      const float errf = rkTrial<float>(P.field, posf, dirf, qopf, (float)h, s);
+      double err = errf;
+      bool accept;
+      if (errf <= tolLo) {
+        accept = true;
+      } else if (errf > tolHi) {
+        accept = false;
+      } else {
+        // undecided in FP32: the FP64 trial decides
+        RkStages<double> sd;
+        rkFirst<double>(P.field, L.pos, L.dir, L.qop, sd);
+        err = rkTrial<double>(P.field, L.pos, L.dir, L.qop, h, sd);
+        accept = err <= P.tol;
+      }
+      if (accept) break;
+      const double scale = smin(smax(0.25, pow(P.tol / fabs(2. * err), 0.25)), 4.);
+      const double hn = h * scale;
+      L.ss[kAccuracy] = hn;
+      L.ssDir = hn > 0. ? 1 : -1;
+      h = ssValue(L);
+      if (h * h < P.cutoff * P.cutoff) return;
+      if (nTrials > P.maxTrials) return;
+      nTrials++;
+    }
+    L.t += h * L.dtds;
+    const float hf = (float)h;
+    transportUpdate<float>(L, dirf, qopf, hf, (float)L.d37, s);
+    // motion: FP64 state plus FP32 increments
+    const float hh6 = hf * hf / 6.f, h6 = hf / 6.f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const float dp = hh6 * (s.k1[i] + s.k2[i] + s.k3[i]);
+      const float dd = h6 * (s.k1[i] + 2.f * (s.k2[i] + s.k3[i]) + s.k4[i]);
+      L.pos[i] = L.pos[i] + (h * L.dir[i] + (double)dp);
+      L.dir[i] = L.dir[i] + (double)dd;
+    }
+    // |dir|^2 = 1 + e with e ~ (h kappa)^2 <= 1e-3: two Newton steps of
+    // 1/sqrt from 1 reach FP64 precision (error ~ e^4)
+    const double n2 = L.dir[0] * L.dir[0] + L.dir[1] * L.dir[1] + L.dir[2] * L.dir[2];
+    double f = 1.5 - 0.5 * n2;
+    f = f * (1.5 - 0.5 * n2 * f * f);
+    if (fabs(n2 - 1.) > 1e-3) f = 1. / sqrt(n2); // large turning steps
+    L.dir[0] *= f;
+    L.dir[1] *= f;
+    L.dir[2] *= f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      L.der[i] = (float)L.dir[i];
+      L.der[4 + i] = s.k4[i];
+    }
+    L.der[3] = (float)L.dtds;
   }
-  L.der[0] = L.dir[0];
-  L.der[1] = L.dir[1];
-  L.der[2] = L.dir[2];
-  L.der[4] = k4[0];
-  L.der[5] = k4[1];
-  L.der[6] = k4[2];
   L.pathAcc += h;
   L.rkSteps++;
 }
@@ -433,11 +588,12 @@ __device__ void rkStep(Lane &L, const Params &P) {
 //   Dd[r][c]  rows 4-6, cols 0..4
 // Row 7 is e4 and column 5 is e3 throughout.
 // ---------------------------------------------------------------------------
-struct Transported {
-  double Pt[3][5], R3[5], Dd[3][5];
+template <typename R> struct Transported {
+  R Pt[3][5], R3[5], Dd[3][5];
 };
 
-__device__ __forceinline__ void applyTransport(const Lane &L, Transported &X) {
+template <typename R>
+__device__ __forceinline__ void applyTransport(const Lane<R> &L, Transported<R> &X) {
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
     X.Pt[r][0] = L.G03[r][0];
@@ -450,24 +606,24 @@ __device__ __forceinline__ void applyTransport(const Lane &L, Transported &X) {
                        L.JB[r][2] * L.G46[2][c];
     }
     X.Pt[r][4] = L.Ja[r];
-    X.Dd[r][0] = 0.;
-    X.Dd[r][1] = 0.;
+    X.Dd[r][0] = R(0);
+    X.Dd[r][1] = R(0);
     X.Dd[r][4] = L.Jc[r];
   }
-  X.R3[0] = 0.;
-  X.R3[1] = 0.;
-  X.R3[2] = 0.;
-  X.R3[3] = 0.;
+  X.R3[0] = R(0);
+  X.R3[1] = R(0);
+  X.R3[2] = R(0);
+  X.R3[3] = R(0);
   X.R3[4] = L.Jb;
 }
 
-// jacToGlobal -= derivative * sVec, then J = jacToLocal * jacToGlobal and
-// cov <- J cov J^T.  axis0/axis1 are the surface's local measurement axes
+// jacToGlobal -= derivative * sVec, then J = jacToLocal * jacToGlobal (in R)
+// and cov <- J cov J^T (in FP64).  ax0/ax1 are the surface's local axes
 // (rows 0 and 1 of jacToLocal); the direction rows follow
 // PlaneSurface.ipp:158-189 / LineSurface.ipp:114-143.
-__device__ __forceinline__ void projectCov(Lane &L, Transported &X, const double sVec[5],
-                                           const double ax0[3], const double ax1[3],
-                                           double Jst[25]) {
+template <typename R>
+__device__ __forceinline__ void projectCov(Lane<R> &L, Transported<R> &X, const R sVec[5],
+                                           const R ax0[3], const R ax1[3], double Jst[25]) {
 #pragma unroll
   for (int c = 0; c < 5; ++c) {
 #pragma unroll
@@ -477,12 +633,12 @@ __device__ __forceinline__ void projectCov(Lane &L, Transported &X, const double
     }
     X.R3[c] -= L.der[3] * sVec[c];
   }
-  const double x = L.dir[0], y = L.dir[1], z = L.dir[2];
-  const double cosT = z, sinT = sqrt(x * x + y * y);
-  const double invS = 1. / sinT;
-  const double cosP = x * invS, sinP = y * invS;
-  const double j24 = -sinP * invS, j25 = cosP * invS;
-  const double j34 = cosP * cosT, j35 = sinP * cosT, j36 = -sinT;
+  const R x = (R)L.dir[0], y = (R)L.dir[1], z = (R)L.dir[2];
+  const R cosT = z, sinT = sqrt(x * x + y * y);
+  const R invS = R(1) / sinT;
+  const R cosP = x * invS, sinP = y * invS;
+  const R j24 = -sinP * invS, j25 = cosP * invS;
+  const R j34 = cosP * cosT, j35 = sinP * cosT, j36 = -sinT;
   double J[6][6];
 #pragma unroll
   for (int c = 0; c < 5; ++c) {
@@ -541,7 +697,8 @@ __device__ __forceinline__ void projectCov(Lane &L, Transported &X, const double
 
 // BoundParameters from the free state (CovarianceEngine.hpp:363-370 and
 // coordinate_transformations.hpp:115-128): angles and q/p from the momentum.
-__device__ __forceinline__ void boundAngles(const Lane &L, double out[6], double mom[3]) {
+template <typename R>
+__device__ __forceinline__ void boundAngles(const Lane<R> &L, double out[6], double mom[3]) {
   const double qopF = L.q / L.p;
   const double pabs = fabs(1. / qopF);
   mom[0] = pabs * L.dir[0];
@@ -557,16 +714,20 @@ __device__ __forceinline__ void boundAngles(const Lane &L, double out[6], double
 }
 
 // boundState<PlaneSurface> (EigenStepper.ipp:516-540) incl. re-initialisation
-__device__ void boundStatePlane(Lane &L, const PlaneD &pl, double out[6], double Jst[25]) {
-  Transported X;
+template <typename R>
+__device__ void boundStatePlane(Lane<R> &L, const PlaneD &pl, double out[6], double Jst[25]) {
+  Transported<R> X;
   applyTransport(L, X);
   // PlaneSurface::derivativeFactors (PlaneSurface.ipp:191-204)
-  const double dp = pl.T[0] * L.dir[0] + pl.T[1] * L.dir[1] + pl.T[2] * L.dir[2];
-  const double nv0 = pl.T[0] / dp, nv1 = pl.T[1] / dp, nv2 = pl.T[2] / dp;
-  double sVec[5];
+  const R T0 = (R)pl.T[0], T1 = (R)pl.T[1], T2 = (R)pl.T[2];
+  const R dp = T0 * (R)L.dir[0] + T1 * (R)L.dir[1] + T2 * (R)L.dir[2];
+  const R nv0 = T0 / dp, nv1 = T1 / dp, nv2 = T2 / dp;
+  R sVec[5];
 #pragma unroll
   for (int c = 0; c < 5; ++c) sVec[c] = nv0 * X.Pt[0][c] + nv1 * X.Pt[1][c] + nv2 * X.Pt[2][c];
-  projectCov(L, X, sVec, pl.U, pl.V, Jst);
+  const R U[3] = {(R)pl.U[0], (R)pl.U[1], (R)pl.U[2]};
+  const R V[3] = {(R)pl.V[0], (R)pl.V[1], (R)pl.V[2]};
+  projectCov(L, X, sVec, U, V, Jst);
   // reinitializeJacobians (CovarianceEngine.hpp:169-201)
   resetTransport(L);
   planeJacToGlobal(L, pl);
@@ -578,28 +739,31 @@ __device__ void boundStatePlane(Lane &L, const PlaneD &pl, double out[6], double
 }
 
 // boundState<LineSurface> towards the perigee line (axis z through `c`)
-__device__ void boundStateLine(Lane &L, const double c[3], double out[6]) {
-  Transported X;
+template <typename R>
+__device__ void boundStateLine(Lane<R> &L, const double c[3], double out[6]) {
+  Transported<R> X;
   applyTransport(L, X);
   double mX[3], mY[3], mD[3];
   lineFrame(L.dir, mX, mY, mD);
   // LineSurface::derivativeFactors (LineSurface.ipp:145-182), locz = (0,0,1)
   const double pc0 = L.pos[0] - c[0], pc1 = L.pos[1] - c[1], pc2 = L.pos[2] - c[2];
-  const double long_c = mY[0] * L.dir[0] + mY[1] * L.dir[1] + mY[2] * L.dir[2];
-  const double nv0 = L.dir[0] - long_c * mY[0], nv1 = L.dir[1] - long_c * mY[1],
-               nv2 = L.dir[2] - long_c * mY[2];
-  const double nrm = 1. / (1. - long_c * long_c);
-  double sVec[5];
+  const R rY[3] = {(R)mY[0], (R)mY[1], (R)mY[2]};
+  const R rX[3] = {(R)mX[0], (R)mX[1], (R)mX[2]};
+  const R dr[3] = {(R)L.dir[0], (R)L.dir[1], (R)L.dir[2]};
+  const R long_c = rY[0] * dr[0] + rY[1] * dr[1] + rY[2] * dr[2];
+  const R nv0 = dr[0] - long_c * rY[0], nv1 = dr[1] - long_c * rY[1], nv2 = dr[2] - long_c * rY[2];
+  const R nrm = R(1) / (R(1) - long_c * long_c);
+  const R p0 = (R)pc0, p1 = (R)pc1, p2 = (R)pc2;
+  R sVec[5];
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
-    const double s = nv0 * X.Pt[0][k] + nv1 * X.Pt[1][k] + nv2 * X.Pt[2][k];
-    const double e0 = mY[0] * s - X.Dd[0][k], e1 = mY[1] * s - X.Dd[1][k],
-                 e2 = mY[2] * s - X.Dd[2][k];
-    const double row = pc0 * e0 + pc1 * e1 + pc2 * e2;
+    const R s = nv0 * X.Pt[0][k] + nv1 * X.Pt[1][k] + nv2 * X.Pt[2][k];
+    const R e0 = rY[0] * s - X.Dd[0][k], e1 = rY[1] * s - X.Dd[1][k], e2 = rY[2] * s - X.Dd[2][k];
+    const R row = p0 * e0 + p1 * e1 + p2 * e2;
     sVec[k] = nrm * (s - row);
   }
   double Jst[25];
-  projectCov(L, X, sVec, mX, mY, Jst);
+  projectCov(L, X, sVec, rX, rY, Jst);
   double mom[3];
   boundAngles(L, out, mom);
   // LineSurface::globalToLocal (LineSurface.ipp:200-220)
@@ -612,7 +776,8 @@ __device__ void boundStateLine(Lane &L, const double c[3], double out[6]) {
 
 // EigenStepper::update (EigenStepper.ipp:554-564) from bound parameters on a
 // plane (boundParameters2freeParameters, coordinate_transformations.hpp:145-158)
-__device__ __forceinline__ void stepperUpdate(Lane &L, const PlaneD &pl, const double par[6],
+template <typename R>
+__device__ __forceinline__ void stepperUpdate(Lane<R> &L, const PlaneD &pl, const double par[6],
                                               const double cov[21], double mass) {
 #pragma unroll
   for (int r = 0; r < 3; ++r) L.pos[r] = pl.U[r] * par[0] + pl.V[r] * par[1] + pl.c[r];
@@ -634,15 +799,20 @@ __device__ __forceinline__ void stepperUpdate(Lane &L, const PlaneD &pl, const d
 // ---------------------------------------------------------------------------
 // Workspace access: state s of track i, element e
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double *wsPtr(const Params &P, const Lane &L, int s, int e) {
+template <typename R>
+__device__ __forceinline__ double *wsPtr(const Params &P, const Lane<R> &L, int s, int e) {
   return P.ws + ((size_t)s * kStateStride + e) * (size_t)P.wsStride + L.idx;
 }
 
 // ---------------------------------------------------------------------------
 // Actor::filter (KalmanFitter.hpp:284-350) for a plane that has a hit, with
-// GainMatrixUpdater (GainMatrixUpdater.hpp:34-106)
+// GainMatrixUpdater (GainMatrixUpdater.hpp:34-106).  The plain form keeps the
+// reference's (I - KH) C update; the mixed form uses the Joseph form
+// (I - KH) C (I - KH)^T + K V K^T, which stays positive definite when the
+// predicted covariance carries FP32-level errors from the Jacobian.
 // ---------------------------------------------------------------------------
-__device__ void filterHit(Lane &L, const Params &P, const PlaneD *planes, int k) {
+template <typename R>
+__device__ void filterHit(Lane<R> &L, const Params &P, const PlaneD *planes, int k) {
   const PlaneD &pl = planes[k];
   double pred[6], Jst[25];
   boundStatePlane(L, pl, pred, Jst);
@@ -678,11 +848,32 @@ __device__ void filterHit(Lane &L, const Params &P, const PlaneD *planes, int k)
     double filt[6], cf[21];
 #pragma unroll
     for (int i = 0; i < 6; ++i) filt[i] = pred[i] + (K0[i] * r0 + K1[i] * r1);
+    if constexpr (sizeof(R) == sizeof(double)) {
 #pragma unroll
-    for (int i = 0; i < 6; ++i) {
+      for (int i = 0; i < 6; ++i) {
 #pragma unroll
-      for (int j = i; j < 6; ++j)
-        cf[ut(i, j)] = L.cov[ut(i, j)] - K0[i] * L.cov[sidx(0, j)] - K1[i] * L.cov[sidx(1, j)];
+        for (int j = i; j < 6; ++j)
+          cf[ut(i, j)] = L.cov[ut(i, j)] - K0[i] * L.cov[sidx(0, j)] - K1[i] * L.cov[sidx(1, j)];
+      }
+    } else {
+      // Joseph form with H = [I2 0]:
+      //   C - K A - A^T K^T + K (S0 + V) K^T,  A = H C, S0 + V = S
+      double KS0[6], KS1[6];
+#pragma unroll
+      for (int i = 0; i < 6; ++i) {
+        KS0[i] = K0[i] * S00 + K1[i] * S10;
+        KS1[i] = K0[i] * S01 + K1[i] * S11;
+      }
+#pragma unroll
+      for (int i = 0; i < 6; ++i) {
+#pragma unroll
+        for (int j = i; j < 6; ++j) {
+          const double ka = K0[i] * L.cov[sidx(0, j)] + K1[i] * L.cov[sidx(1, j)];
+          const double ak = K0[j] * L.cov[sidx(0, i)] + K1[j] * L.cov[sidx(1, i)];
+          const double ksk = KS0[i] * K0[j] + KS1[i] * K1[j];
+          cf[ut(i, j)] = (L.cov[ut(i, j)] - ka) - (ak - ksk);
+        }
+      }
     }
 #pragma unroll
     for (int e = 0; e < 6; ++e) *wsPtr(P, L, s, 6 + e) = filt[e];
@@ -770,7 +961,8 @@ __device__ __forceinline__ void invJacobian(const double J[25], double Gi[25]) {
 // 5e-8 relative between two valid FP64 evaluations), and without storing
 // covariances per state.
 // ---------------------------------------------------------------------------
-__device__ bool finalizeSmooth(Lane &L, const Params &P, const PlaneD *planes) {
+template <typename R>
+__device__ bool finalizeSmooth(Lane<R> &L, const Params &P, const PlaneD *planes) {
   L.smoothed = true;
   const int n = L.measStates;
   double xs[6], Cs[21];
@@ -873,7 +1065,8 @@ __device__ bool finalizeSmooth(Lane &L, const Params &P, const PlaneD *planes) {
 // ---------------------------------------------------------------------------
 // Navigation (DirectNavigator.hpp:158-225, SteppingHelper.hpp:31-65)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ int updateSurfaceStatus(Lane &L, const Params &P, const PlaneD &pl) {
+template <typename R>
+__device__ __forceinline__ int updateSurfaceStatus(Lane<R> &L, const Params &P, const PlaneD &pl) {
   const double d0 = L.navDir * L.dir[0], d1 = L.navDir * L.dir[1], d2 = L.navDir * L.dir[2];
   const double denom = d0 * pl.T[0] + d1 * pl.T[1] + d2 * pl.T[2];
   if (denom != 0.0) {
@@ -894,7 +1087,8 @@ __device__ __forceinline__ int updateSurfaceStatus(Lane &L, const Params &P, con
   return kMissed;
 }
 
-__device__ __forceinline__ void navStatus(Lane &L, const Params &P, const PlaneD *planes) {
+template <typename R>
+__device__ __forceinline__ void navStatus(Lane<R> &L, const Params &P, const PlaneD *planes) {
   L.current = -1;
   if (L.next != L.nSeq) {
     if (updateSurfaceStatus(L, P, planes[L.next]) == kOnSurface) {
@@ -905,7 +1099,8 @@ __device__ __forceinline__ void navStatus(Lane &L, const Params &P, const PlaneD
   }
 }
 
-__device__ __forceinline__ void navTarget(Lane &L, const Params &P, const PlaneD *planes) {
+template <typename R>
+__device__ __forceinline__ void navTarget(Lane<R> &L, const Params &P, const PlaneD *planes) {
   L.current = -1;
   if (L.next != L.nSeq) {
     if (updateSurfaceStatus(L, P, planes[L.next]) == kMissed) ++L.next;
@@ -915,7 +1110,8 @@ __device__ __forceinline__ void navTarget(Lane &L, const Params &P, const PlaneD
 }
 
 // LineSurface::intersect (LineSurface.ipp:229-262) along navDir * dir
-__device__ __forceinline__ void lineIntersect(const Lane &L, const Params &P, double &u,
+template <typename R>
+__device__ __forceinline__ void lineIntersect(const Lane<R> &L, const Params &P, double &u,
                                               int &status) {
   const double ea0 = L.navDir * L.dir[0], ea1 = L.navDir * L.dir[1], ea2 = L.navDir * L.dir[2];
   const double m0 = L.perigee[0] - L.pos[0], m1 = L.perigee[1] - L.pos[1],
@@ -936,7 +1132,8 @@ __device__ __forceinline__ void lineIntersect(const Lane &L, const Params &P, do
 // runs when no filter update, smoothing or final transport is due, and
 // returns false without touching the state otherwise.
 // ---------------------------------------------------------------------------
-__device__ bool actor(Lane &L, const Params &P, const PlaneD *planes, bool heavy) {
+template <typename R>
+__device__ bool actor(Lane<R> &L, const Params &P, const PlaneD *planes, bool heavy) {
   const bool onPlane = L.current >= 0 && !L.smoothed && !L.finished;
   const bool hit = onPlane && ((L.mask >> L.current) & 1ull);
   if (!heavy) {
@@ -996,7 +1193,7 @@ __device__ bool actor(Lane &L, const Params &P, const PlaneD *planes, bool heavy
 
 // Kalman aborter (KalmanFitter.hpp:682-694) then PathLimitReached
 // (StandardAborters.hpp:37-56)
-__device__ __forceinline__ bool aborters(Lane &L, const Params &P) {
+template <typename R> __device__ __forceinline__ bool aborters(Lane<R> &L, const Params &P) {
   if (!L.result || L.finished) return true;
   if (L.targetReached) return true;
   const double distance = L.navDir * fabs(DBL_MAX) - L.pathAcc;
@@ -1006,7 +1203,7 @@ __device__ __forceinline__ bool aborters(Lane &L, const Params &P) {
   return limit;
 }
 
-__device__ __forceinline__ void finish(Lane &L, const Params &P) {
+template <typename R> __device__ __forceinline__ void finish(Lane<R> &L, const Params &P) {
   int st;
   if (!L.result)
     st = L.smoothed ? KF_TRACK_SMOOTHER_NAN : KF_TRACK_MEAS_MISMATCH;
@@ -1027,7 +1224,7 @@ __device__ __forceinline__ void finish(Lane &L, const Params &P) {
 // (heavy actor work) is due, or the track is done; runEvent() executes the
 // pending actor call with heavy work allowed and continues.
 // ---------------------------------------------------------------------------
-__device__ void advance(Lane &L, const Params &P, const PlaneD *planes) {
+template <typename R> __device__ void advance(Lane<R> &L, const Params &P, const PlaneD *planes) {
   for (;;) {
     switch (L.pc) {
     case PC_PRE:
@@ -1080,7 +1277,7 @@ __device__ void advance(Lane &L, const Params &P, const PlaneD *planes) {
   }
 }
 
-__device__ void runEvent(Lane &L, const Params &P, const PlaneD *planes) {
+template <typename R> __device__ void runEvent(Lane<R> &L, const Params &P, const PlaneD *planes) {
   L.parked = false;
   switch (L.pc) {
   case PC_PRE:
@@ -1115,7 +1312,8 @@ __device__ void runEvent(Lane &L, const Params &P, const PlaneD *planes) {
 
 // EigenStepper::State from BoundParameters<LineSurface> (EigenStepper.hpp:40-61)
 // and the navigator initialisation; returns false for unusable input.
-__device__ void initLane(Lane &L, const Params &P, const PlaneD *planes, int64_t i) {
+template <typename R>
+__device__ void initLane(Lane<R> &L, const Params &P, const PlaneD *planes, int64_t i) {
   L.idx = i;
   L.pc = PC_DONE;
   L.parked = false;
@@ -1189,21 +1387,17 @@ __device__ void initLane(Lane &L, const Params &P, const PlaneD *planes, int64_t
     const double cosP = x * inv, sinP = y * inv;
     double X[3], Y[3], D[3];
     lineFrame(L.dir, X, Y, D);
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-      L.G03[r][0] = X[r];
-      L.G03[r][1] = Y[r];
-    }
-    L.G46[0][0] = (-sinT) * sinP;
-    L.G46[0][1] = cosT * cosP;
-    L.G46[1][0] = sinT * cosP;
-    L.G46[1][1] = cosT * sinP;
-    L.G46[2][0] = 0.;
-    L.G46[2][1] = (-sinT);
+    double G46[3][2];
+    G46[0][0] = (-sinT) * sinP;
+    G46[0][1] = cosT * cosP;
+    G46[1][0] = sinT * cosP;
+    G46[1][1] = cosT * sinP;
+    G46[2][0] = 0.;
+    G46[2][1] = (-sinT);
     const double ipdn = 1. / (L.dir[0] * D[0] + L.dir[1] * D[1] + L.dir[2] * D[2]);
     double dP[3], dT[3];
-    const double cphi[3] = {L.G46[0][0], L.G46[1][0], L.G46[2][0]};
-    const double cth_[3] = {L.G46[0][1], L.G46[1][1], L.G46[2][1]};
+    const double cphi[3] = {G46[0][0], G46[1][0], G46[2][0]};
+    const double cth_[3] = {G46[0][1], G46[1][1], G46[2][1]};
     cross3(Y, cphi, dP);
     cross3(Y, cth_, dT);
     const double xp = X[0] * dP[0] + X[1] * dP[1] + X[2] * dP[2];
@@ -1212,8 +1406,12 @@ __device__ void initLane(Lane &L, const Params &P, const PlaneD *planes, int64_t
     for (int r = 0; r < 3; ++r) {
       dP[r] = dP[r] - xp * X[r];
       dT[r] = dT[r] - xt * X[r];
-      L.G03[r][2] = dP[r] * sp[0] * ipdn;
-      L.G03[r][3] = dT[r] * sp[0] * ipdn;
+      L.G03[r][0] = (R)X[r];
+      L.G03[r][1] = (R)Y[r];
+      L.G03[r][2] = (R)(dP[r] * sp[0] * ipdn);
+      L.G03[r][3] = (R)(dT[r] * sp[0] * ipdn);
+      L.G46[r][0] = (R)G46[r][0];
+      L.G46[r][1] = (R)G46[r][1];
     }
   }
   L.pc = PC_PRE;

@@ -215,7 +215,7 @@ void kf_synth_config_default(kf_synth_config_t *c) {
   c->seed_time_sigma = 5. * 299.792458; // 5 ns (Run/Common/Processor.hpp:31)
   c->mis_shift_sigma = 0.;
   c->mis_rot_sigma = 0.;
-  c->rk_step = 2.;
+  c->rk_step = 5.;
 }
 
 int32_t kf_synth_geometry(const kf_synth_config_t *cfg, double *center,

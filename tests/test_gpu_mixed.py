@@ -1,0 +1,52 @@
+"""The mixed-precision form (FP32 propagation and Jacobians, FP64 Kalman
+algebra) against the FP64 oracle: same control flow on almost every track,
+small parameter errors, identical pull widths."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+DIAG = [0, 6, 11, 15, 18, 20]
+
+
+def _errors(g, o):
+    ok = (o["status"] == 0) & (g["status"] == 0)
+    sig = np.sqrt(np.abs(o["cov"][DIAG]))[:, ok]
+    scale = np.maximum(np.abs(o["params"][:, ok]), sig)
+    return ok, np.abs(g["params"][:, ok] - o["params"][:, ok]) / scale
+
+
+def _pull_widths(r, tel, ok):
+    return ((r["params"] - tel.truth) / np.sqrt(np.abs(r["cov"][DIAG])))[:5, ok].std(axis=1)
+
+
+@pytest.mark.parametrize("workload", ["uniform10", "map30"])
+def test_mixed_against_fp64_oracle(kf, orc, workload):
+    kw = {} if workload == "uniform10" else dict(n_planes=30, x_first=50., x_step=50.,
+                                                  field_map=True)
+    tel = kf.make_telescope(20_000, seed=77, **kw)
+    g = kf.fit_device(tel, kf.default_config(overstep_limit=0.1, precision=1))
+    o = orc.fit(tel, kf.default_config(overstep_limit=0.1), threads=0, variant="precise")
+    assert np.mean(g["status"] == o["status"]) >= 0.999
+    assert np.mean(g["n_steps"] == o["n_steps"]) >= 0.995
+    ok, rel = _errors(g, o)
+    med = np.median(rel, axis=1)
+    p99 = np.percentile(rel, 99, axis=1)
+    print("median", med, "p99", p99, "max", rel.max(axis=1))
+    assert np.all(med <= 1e-5), med
+    assert np.all(p99 <= 1e-4), p99
+    wg, wo = _pull_widths(g, tel, ok), _pull_widths(o, tel, ok)
+    assert np.all(np.abs(wg / wo - 1) < 0.01), (wg, wo)
+
+
+def test_mixed_holes_outliers(kf, orc):
+    tel = kf.make_telescope(20_000, n_planes=30, x_first=50., x_step=50., min_len=5, max_len=30,
+                           hit_prob=0.9, outlier_prob=0.02, seed=11)
+    cfg64 = kf.default_config(overstep_limit=0.1, outlier_chi2_cut=25.0)
+    cfg = kf.default_config(overstep_limit=0.1, outlier_chi2_cut=25.0, precision=1)
+    g = kf.fit_device(tel, cfg)
+    o = orc.fit(tel, cfg64, threads=0, variant="precise")
+    assert np.mean(g["status"] == o["status"]) >= 0.999
+    assert np.mean(g["n_meas"] == o["n_meas"]) >= 0.999
+    ok, rel = _errors(g, o)
+    assert np.all(np.median(rel, axis=1) <= 1e-5)
