@@ -21,7 +21,7 @@ LIBDIR = PKG / "_lib"
 LIB = LIBDIR / "libgb300kf.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["kf_capi.cu", "kf_fit_fp64.cu", "kf_fit_mixed.cu", "kf_diag.cu"]
+CU_SOURCES = ["kf_capi.cu", "kf_fit_fp64.cu", "kf_fit_mixed.cu", "kf_diag.cu", "kf_noalloc.cu"]
 CXX_SOURCES = ["synth.cpp"]
 
 

@@ -194,6 +194,29 @@ int32_t kf_fit_batch_host(const kf_inputs_t *host_in, kf_outputs_t *host_out,
                           const kf_field_t *field, void *device_staging,
                           size_t staging_bytes, void *stream);
 
+/* ---- fitting without allocation ------------------------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * (a host framework owns all device memory through its own pool, a plugin
+ * host forbids foreign allocations, or cudaMalloc's implicit synchronisation
+ * or mid-run failure is unacceptable): same inputs and outputs as
+ * kf_fit_batch, with the workspace taken from a static device array of
+ * KF_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until the
+ * process exits.  A batch needing more scratch than that (kf_workspace_size)
+ * is rejected with KF_ERR_WORKSPACE_TOO_SMALL and a message from
+ * kf_noalloc_last_error_string(); split it or use kf_fit_batch.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the one array: calls that overlap on the GPU (different
+ * streams, or host threads without ordering) race on it.  Nothing is
+ * allocated, and nothing needs clearing between calls. */
+#define KF_NOALLOC_SCRATCH_BYTES (64ull << 20)
+
+int32_t kf_fit_batch_noalloc(const kf_inputs_t *in, kf_outputs_t *out,
+                             const kf_config_t *cfg, const kf_geometry_t *geo,
+                             const kf_field_t *field, void *stream);
+size_t kf_noalloc_scratch_bytes(void);
+const char *kf_noalloc_last_error_string(void);
+
 #ifdef __cplusplus
 }
 #endif
