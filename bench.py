@@ -31,19 +31,41 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-METRIC = "fitted tracks/s (plain FP64 Kalman fit: RK4 propagation + gain-matrix filter + RTS smoother + perigee transport)"
+METRIC = "fitted tracks/s (Kalman fit: RK4 propagation + gain-matrix filter + RTS smoother + perigee transport)"
 UNIT = "tracks/s"
 OVERSTEP = 0.1  # mm; the reference's fixed 0.01 mm skips planes on this workload
 CPU_SAMPLE = 100_000
 
+# workload name -> (description, make_telescope keyword arguments, fit config extras)
+WORKLOADS = {
+    "uniform10": ("telescope of 10 planes x=100..1000 mm, uniform 2 T, pi+- |p| 1-10 GeV, "
+                  "50 um hits, seeds 50 um/1 mrad/5 %", {}, {}),
+    "map30": ("telescope of 30 planes x=50..1500 mm, 101^3 FP32 field map over +-1.5 m "
+              "(Bz = 2 T (1 - 0.2 (r/1.5 m)^2) exp(-(z/3 m)^2), Br from div B = 0), trilinear",
+              dict(n_planes=30, x_first=50., x_step=50., field_map=True), {}),
+    "holes30": ("telescope of 30 planes x=50..1500 mm, uniform 2 T, path length U{5..30} planes, "
+                "hit probability 0.9, 2 % outliers shifted U(+-5 mm), outlier chi2 cut 25",
+                dict(n_planes=30, x_first=50., x_step=50., min_len=5, max_len=30, hit_prob=0.9,
+                     outlier_prob=0.02), dict(outlier_chi2_cut=25.0)),
+}
+PRECISIONS = {"fp64": 0, "mixed": 1}
 
-def workload_config(n_tracks: int) -> dict:
-    return {"workload": "plain FP64 fit at scale: telescope of 10 planes x=100..1000 mm, uniform 2 T, "
-                        "pi+- |p| 1-10 GeV, 50 um hits, seeds 50 um/1 mrad/5 %",
-            "tracks_per_gpu": n_tracks, "planes": 10, "field": "uniform 2 T along z",
-            "precision": "fp64", "overstep_limit_mm": OVERSTEP, "rk_tolerance": 1e-4,
+
+def workload_config(name: str, n_tracks: int, precision: str) -> dict:
+    desc, kw, _ = WORKLOADS[name]
+    return {"workload": f"{name}: {desc}", "tracks_per_gpu": n_tracks,
+            "precision": precision, "overstep_limit_mm": OVERSTEP, "rk_tolerance": 1e-4,
             "mass_in_fit": "muon (reference default)",
-            "l2": "inputs (~0.65 GB per 1M tracks) larger than the 129 MB L2"}
+            "l2": "inputs larger than the 129 MB L2 at 1M tracks"}
+
+
+def make_workload(kf, name: str, n: int, seed: int):
+    return kf.make_telescope(n, seed=seed, **WORKLOADS[name][1])
+
+
+def fit_config(kf, name: str, precision: str):
+    return kf.default_config(overstep_limit=OVERSTEP, precision=PRECISIONS[precision],
+                             **WORKLOADS[name][2])
 
 
 def env_rank():
@@ -52,12 +74,13 @@ def env_rank():
 
 
 # ---------------------------------------------------------------------------
-def cpu_oracle_rate(n_tracks: int, reps: int, warmup: int, seed: int) -> dict:
+def cpu_oracle_rate(n_tracks: int, reps: int, warmup: int, seed: int,
+                    workload: str = "uniform10") -> dict:
     """The reference algorithm on the host cores (oracle port)."""
     import gpukalmanfitter_gb300 as kf
     import oracle
-    tel = kf.make_telescope(n_tracks, seed=seed)
-    cfg = kf.default_config(overstep_limit=OVERSTEP)
+    tel = make_workload(kf, workload, n_tracks, seed)
+    cfg = fit_config(kf, workload, "fp64")
     lib = oracle.load()
     threads = int(lib.oracle_num_threads())
     for _ in range(warmup):
@@ -78,12 +101,13 @@ def run_reference(args) -> None:
     rank, world, _ = env_rank()
     if rank != 0:
         return
-    base = cpu_oracle_rate(CPU_SAMPLE, args.steps, args.warmup, seed=1234567890)
+    base = cpu_oracle_rate(CPU_SAMPLE, args.steps, args.warmup, seed=1234567890,
+                           workload=args.workload)
     line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": UNIT,
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": base["seconds_per_step"] * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {**workload_config(CPU_SAMPLE),
+            "config": {**workload_config(args.workload, CPU_SAMPLE, "fp64"),
                        "note": "reference algorithm restated in C++ FP64 (oracle/kf_oracle.cpp); "
                                "the reference binary needs Eigen3/Boost/ROOT, absent here"},
             "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")},
@@ -155,8 +179,8 @@ def run_gpu(args) -> None:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     n = args.tracks
-    tel = kf.make_telescope(n, seed=1234567890 + rank)
-    cfg = kf.default_config(overstep_limit=OVERSTEP)
+    tel = make_workload(kf, args.workload, n, 1234567890 + rank)
+    cfg = fit_config(kf, args.workload, args.precision)
     lib = kf.load()
 
     stream = torch.cuda.Stream()
@@ -207,18 +231,18 @@ def run_gpu(args) -> None:
     achieved = flop / avg_launch_s / 1e12
     traffic = None
     tfile = ROOT / "profiles" / "traffic_fp64_fit.json"
-    if tfile.exists():
+    if tfile.exists() and args.workload == "uniform10" and args.precision == "fp64":
         try:
             traffic = json.loads(tfile.read_text())["dram_bytes_per_track"] * n
         except Exception:
             traffic = None
 
     # ---- end to end through the public host-buffer call (pinned memory)
-    e2e = run_e2e(kf, lib, tel, cfg, stream, args, barrier, dist)
+    e2e = None if args.no_e2e else run_e2e(kf, lib, tel, cfg, stream, args, barrier, dist)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_oracle_rate(CPU_SAMPLE, 3, 1, seed=1234567890)
+        cpu = cpu_oracle_rate(CPU_SAMPLE, 3, 1, seed=1234567890, workload=args.workload)
         cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
 
     if rank == 0:
@@ -226,9 +250,11 @@ def run_gpu(args) -> None:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else "f32+f64",
             "data": "synthetic (seeded generator, analytic-helix truth)",
-            "config": {**workload_config(n), "parallelism": f"track shards, {world} GPU(s), no collective"},
+            "config": {**workload_config(args.workload, n, args.precision),
+                       "parallelism": f"track shards, {world} GPU(s), no collective"},
             "fitted_fraction": ok_frac,
             "gpu_launches": args.steps,
             "e2e": e2e,
@@ -315,7 +341,10 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--tracks", type=int, default=1_000_000, help="tracks per GPU")
+    ap.add_argument("--workload", default="uniform10", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="fp64", choices=sorted(PRECISIONS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -44,7 +44,7 @@ class KfConfig(C.Structure):
                 ("mass", C.c_double), ("overstep_limit", C.c_double),
                 ("on_surface_tol", C.c_double), ("outlier_chi2_cut", C.c_double),
                 ("faithful_jacobian", C.c_int32), ("kernel", C.c_int32),
-                ("block_size", C.c_int32), ("reserved0", C.c_int32)]
+                ("block_size", C.c_int32), ("min_blocks_per_sm", C.c_int32)]
 
 
 class KfGeometry(C.Structure):
@@ -87,7 +87,9 @@ class SynthConfig(C.Structure):
 
 _LIB = None
 EXPORTS = ["kf_version", "kf_last_error_string", "kf_config_default", "kf_workspace_size",
-           "kf_fit_batch", "kf_host_staging_size", "kf_fit_batch_host",
+           "kf_fit_batch", "kf_host_staging_size", "kf_fit_batch_host", "kf_batch_workspace_size",
+           "kf_fit_batch_sorted", "kf_batch_plan_create", "kf_batch_plan_launch",
+           "kf_batch_plan_destroy", "kf_autotune",
            "kf_synth_config_default", "kf_synth_geometry", "kf_synth_field_map",
            "kf_synth_tracks"]
 
@@ -116,6 +118,18 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.kf_host_staging_size.argtypes = [C.POINTER(KfConfig), C.c_int64, C.c_int32, C.c_int32]
     lib.kf_fit_batch_host.restype = C.c_int32
     lib.kf_fit_batch_host.argtypes = lib.kf_fit_batch.argtypes
+    lib.kf_batch_workspace_size.restype = C.c_size_t
+    lib.kf_batch_workspace_size.argtypes = [C.POINTER(KfConfig), C.c_int64, C.c_int32]
+    lib.kf_fit_batch_sorted.restype = C.c_int32
+    lib.kf_fit_batch_sorted.argtypes = lib.kf_fit_batch.argtypes
+    lib.kf_batch_plan_create.restype = C.c_int32
+    lib.kf_batch_plan_create.argtypes = [C.POINTER(C.c_void_p)] + lib.kf_fit_batch.argtypes
+    lib.kf_batch_plan_launch.restype = C.c_int32
+    lib.kf_batch_plan_launch.argtypes = [C.c_void_p, C.c_void_p]
+    lib.kf_batch_plan_destroy.argtypes = [C.c_void_p]
+    lib.kf_autotune.restype = C.c_int32
+    lib.kf_autotune.argtypes = lib.kf_fit_batch.argtypes + [C.POINTER(KfConfig),
+                                                            C.POINTER(C.c_double)]
     lib.kf_synth_config_default.argtypes = [C.POINTER(SynthConfig)]
     lib.kf_synth_geometry.restype = C.c_int32
     lib.kf_synth_field_map.restype = C.c_int32
@@ -335,8 +349,10 @@ class DeviceBatch:
         if smoothed:
             self.out["smoothed"] = torch.zeros((S, 27, n), dtype=torch.float64, device=device)
         lib = load()
-        self.ws_bytes = lib.kf_workspace_size(C.byref(self.cfg), n, S)
+        self.ws_bytes = max(lib.kf_workspace_size(C.byref(self.cfg), n, S),
+                            lib.kf_batch_workspace_size(C.byref(self.cfg), n, S))
         self.ws = torch.empty(max(self.ws_bytes, 1), dtype=torch.uint8, device=device)
+        self.plan = None
         self.grid = t(tel.field_grid) if tel.field_grid is not None else None
         self.ins = inputs_struct(self.arrays, n, S, lambda x: x.data_ptr())
         self.outs = _outputs_struct(self.out)
@@ -350,6 +366,53 @@ class DeviceBatch:
                                    C.byref(self.geo), C.byref(self.field),
                                    C.c_void_p(self.ws.data_ptr()), C.c_size_t(self.ws_bytes),
                                    C.c_void_p(s.cuda_stream)))
+
+    def fit_sorted(self, stream=None) -> None:
+        """The batched form: length-sorted queue and persistent kernel."""
+        import torch
+        s = stream if stream is not None else torch.cuda.current_stream()
+        _check(load().kf_fit_batch_sorted(C.byref(self.ins), C.byref(self.outs),
+                                          C.byref(self.cfg), C.byref(self.geo),
+                                          C.byref(self.field), C.c_void_p(self.ws.data_ptr()),
+                                          C.c_size_t(self.ws_bytes), C.c_void_p(s.cuda_stream)))
+
+    def make_plan(self, stream) -> None:
+        """Capture the batched pipeline into a CUDA graph (see kf_batch_plan_create)."""
+        self.destroy_plan()
+        p = C.c_void_p()
+        _check(load().kf_batch_plan_create(C.byref(p), C.byref(self.ins), C.byref(self.outs),
+                                           C.byref(self.cfg), C.byref(self.geo),
+                                           C.byref(self.field), C.c_void_p(self.ws.data_ptr()),
+                                           C.c_size_t(self.ws_bytes),
+                                           C.c_void_p(stream.cuda_stream)))
+        self.plan = p
+
+    def launch_plan(self, stream) -> None:
+        _check(load().kf_batch_plan_launch(self.plan, C.c_void_p(stream.cuda_stream)))
+
+    def destroy_plan(self) -> None:
+        if getattr(self, "plan", None):
+            load().kf_batch_plan_destroy(self.plan)
+            self.plan = None
+
+    def autotune(self, stream=None) -> tuple:
+        """Pick the persistent kernel shape; sets self.cfg and returns (cfg, ms)."""
+        import torch
+        s = stream if stream is not None else torch.cuda.current_stream()
+        tuned = KfConfig()
+        ms = C.c_double(0)
+        _check(load().kf_autotune(C.byref(self.ins), C.byref(self.outs), C.byref(self.cfg),
+                                  C.byref(self.geo), C.byref(self.field),
+                                  C.c_void_p(self.ws.data_ptr()), C.c_size_t(self.ws_bytes),
+                                  C.c_void_p(s.cuda_stream), C.byref(tuned), C.byref(ms)))
+        self.cfg = tuned
+        return tuned, ms.value
+
+    def __del__(self):
+        try:
+            self.destroy_plan()
+        except Exception:
+            pass
 
     def results(self) -> dict:
         return {k: v.cpu().numpy() for k, v in self.out.items()}

@@ -21,7 +21,8 @@ LIBDIR = PKG / "_lib"
 LIB = LIBDIR / "libgb300kf.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["kf_capi.cu", "kf_fit_fp64.cu", "kf_fit_mixed.cu", "kf_diag.cu", "kf_noalloc.cu"]
+CU_SOURCES = ["kf_capi.cu", "kf_fit_fp64.cu", "kf_fit_mixed.cu", "kf_batch.cu", "kf_diag.cu",
+              "kf_noalloc.cu"] + [f"kf_tune_{p}_{m}.cu" for p in ("fp64", "mixed") for m in (2, 3, 5)]
 CXX_SOURCES = ["synth.cpp"]
 
 
@@ -73,7 +74,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         o = obj / (Path(s).stem + ".o")
         objs.append(o)
         jobs.append(["g++", *cxx_flags, "-c", str(CSRC / s), "-o", str(o)])
-    with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+    with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
         for cmd, _ in zip(jobs, ex.map(_run, jobs)):
             if verbose:
                 print(" ".join(cmd))

@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 
+#include "kf_host.h"
 #include "kf_kernels.cuh"
 
 using namespace kfd;
@@ -20,10 +21,14 @@ cudaError_t launchFitFp64(const kfd::Params &P, unsigned grid, cudaStream_t s);
 cudaError_t launchFitMixed(const kfd::Params &P, unsigned grid, cudaStream_t s);
 
 namespace {
-
 thread_local char g_err[512] = "";
+} // namespace
 
-int32_t fail(int32_t code, const char *fmt, const char *detail = "") {
+namespace kfh {
+
+char *errorBuffer() { return g_err; }
+
+int32_t fail(int32_t code, const char *fmt, const char *detail) {
   std::snprintf(g_err, sizeof(g_err), fmt, detail);
   return code;
 }
@@ -116,6 +121,12 @@ void fillParams(Params &P, const kf_inputs_t *in, const kf_outputs_t *out, const
     }
   }
 }
+
+} // namespace kfh
+
+using namespace kfh;
+
+namespace {
 
 int32_t launchFit(const Params &P, int precision, int blockSize, cudaStream_t s) {
   (void)blockSize;

@@ -71,6 +71,8 @@ struct Params {
   double *oParams, *oCov, *oChi2, *oSmoothed;
   int32_t *oStatus, *oNMeas, *oNSteps, *oNTrials;
   double *ws;
+  const int32_t *perm;   // batched form: queue position -> track index
+  int32_t *queueCounter; // batched form: next unclaimed queue position
   FieldD field;
   PlaneD planes[KF_MAX_PLANES];
 };
@@ -205,7 +207,8 @@ template <typename R> struct Lane {
   int pc, steps, status, rkSteps, rkTrials;
   double chi2;
   double perigee[3];
-  int64_t idx;
+  int64_t idx;   // track index (inputs and outputs)
+  int64_t wsIdx; // workspace column (queue position in the batched form)
 };
 
 // ---- ConstrainedStep (ConstrainedStep.hpp:22-108) --------------------------
@@ -801,7 +804,7 @@ __device__ __forceinline__ void stepperUpdate(Lane<R> &L, const PlaneD &pl, cons
 // ---------------------------------------------------------------------------
 template <typename R>
 __device__ __forceinline__ double *wsPtr(const Params &P, const Lane<R> &L, int s, int e) {
-  return P.ws + ((size_t)s * kStateStride + e) * (size_t)P.wsStride + L.idx;
+  return P.ws + ((size_t)s * kStateStride + e) * (size_t)P.wsStride + L.wsIdx;
 }
 
 // ---------------------------------------------------------------------------
@@ -889,24 +892,25 @@ __device__ void filterHit(Lane<R> &L, const Params &P, const PlaneD *planes, int
 //   J^-1 = [[A^-1, -A^-1 b, 0], [0, 1, 0], [-c A^-1, -d + c A^-1 b, 1]]
 // with A^-1 from its 2x2 blocks (Schur complement).  Output rows 0..3 and 5,
 // cols 0..4, in the stored-Jacobian layout.
-__device__ __forceinline__ void invJacobian(const double J[25], double Gi[25]) {
-  const double p00 = J[0], p01 = J[1], p10 = J[5], p11 = J[6];
-  const double q00 = J[2], q01 = J[3], q10 = J[7], q11 = J[8];
-  const double r00 = J[10], r01 = J[11], r10 = J[15], r11 = J[16];
-  const double s00 = J[12], s01 = J[13], s10 = J[17], s11 = J[18];
-  const double rdp = 1. / (p00 * p11 - p01 * p10);
-  const double i00 = p11 * rdp, i01 = -p01 * rdp, i10 = -p10 * rdp, i11 = p00 * rdp;
+template <typename T>
+__device__ __forceinline__ void invJacobian(const T J[25], T Gi[25]) {
+  const T p00 = J[0], p01 = J[1], p10 = J[5], p11 = J[6];
+  const T q00 = J[2], q01 = J[3], q10 = J[7], q11 = J[8];
+  const T r00 = J[10], r01 = J[11], r10 = J[15], r11 = J[16];
+  const T s00 = J[12], s01 = J[13], s10 = J[17], s11 = J[18];
+  const T rdp = T(1) / (p00 * p11 - p01 * p10);
+  const T i00 = p11 * rdp, i01 = -p01 * rdp, i10 = -p10 * rdp, i11 = p00 * rdp;
   // T = P^-1 Q, U = R P^-1
-  const double t00 = i00 * q00 + i01 * q10, t01 = i00 * q01 + i01 * q11;
-  const double t10 = i10 * q00 + i11 * q10, t11 = i10 * q01 + i11 * q11;
-  const double u00 = r00 * i00 + r01 * i10, u01 = r00 * i01 + r01 * i11;
-  const double u10 = r10 * i00 + r11 * i10, u11 = r10 * i01 + r11 * i11;
+  const T t00 = i00 * q00 + i01 * q10, t01 = i00 * q01 + i01 * q11;
+  const T t10 = i10 * q00 + i11 * q10, t11 = i10 * q01 + i11 * q11;
+  const T u00 = r00 * i00 + r01 * i10, u01 = r00 * i01 + r01 * i11;
+  const T u10 = r10 * i00 + r11 * i10, u11 = r10 * i01 + r11 * i11;
   // S' = S - R T, Si = S'^-1
-  const double a00 = s00 - (r00 * t00 + r01 * t10), a01 = s01 - (r00 * t01 + r01 * t11);
-  const double a10 = s10 - (r10 * t00 + r11 * t10), a11 = s11 - (r10 * t01 + r11 * t11);
-  const double rds = 1. / (a00 * a11 - a01 * a10);
-  const double z00 = a11 * rds, z01 = -a01 * rds, z10 = -a10 * rds, z11 = a00 * rds;
-  double Ai[4][4];
+  const T a00 = s00 - (r00 * t00 + r01 * t10), a01 = s01 - (r00 * t01 + r01 * t11);
+  const T a10 = s10 - (r10 * t00 + r11 * t10), a11 = s11 - (r10 * t01 + r11 * t11);
+  const T rds = T(1) / (a00 * a11 - a01 * a10);
+  const T z00 = a11 * rds, z01 = -a01 * rds, z10 = -a10 * rds, z11 = a00 * rds;
+  T Ai[4][4];
   // lower-right Si, lower-left -Si U, upper-right -T Si, upper-left P^-1 + T Si U
   Ai[2][2] = z00;
   Ai[2][3] = z01;
@@ -924,13 +928,13 @@ __device__ __forceinline__ void invJacobian(const double J[25], double Gi[25]) {
   Ai[0][1] = i01 - (t00 * Ai[2][1] + t01 * Ai[3][1]);
   Ai[1][0] = i10 - (t10 * Ai[2][0] + t11 * Ai[3][0]);
   Ai[1][1] = i11 - (t10 * Ai[2][1] + t11 * Ai[3][1]);
-  const double b[4] = {J[4], J[9], J[14], J[19]};
-  const double c[4] = {J[20], J[21], J[22], J[23]};
-  const double d = J[24];
-  double cb = 0.;
+  const T b[4] = {J[4], J[9], J[14], J[19]};
+  const T c[4] = {J[20], J[21], J[22], J[23]};
+  const T d = J[24];
+  T cb = T(0);
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
-    double v = 0.;
+    T v = T(0);
 #pragma unroll
     for (int k = 0; k < 4; ++k) v += Ai[r][k] * b[k];
 #pragma unroll
@@ -940,7 +944,7 @@ __device__ __forceinline__ void invJacobian(const double J[25], double Gi[25]) {
   }
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    double v = 0.;
+    T v = T(0);
 #pragma unroll
     for (int r = 0; r < 4; ++r) v += c[r] * Ai[r][k];
     Gi[20 + k] = -v;
@@ -961,9 +965,119 @@ __device__ __forceinline__ void invJacobian(const double J[25], double Gi[25]) {
 // 5e-8 relative between two valid FP64 evaluations), and without storing
 // covariances per state.
 // ---------------------------------------------------------------------------
+// Mixed-form smoother (no smoothed-state output requested).  The gains
+// G_i = J_i^-1 and the corrections G (x_s' - x_p') are formed in FP32 and
+// added to the FP64 filtered parameters; the smoothed covariance is needed at
+// the first state only, C_s(0) = Pg C_f(n-1) Pg^T with Pg = G_1 ... G_{n-1}
+// accumulated in FP32 on the Jacobian structure.
+template <typename R>
+__device__ bool finalizeSmoothMixed(Lane<R> &L, const Params &P, const PlaneD *planes) {
+  L.smoothed = true;
+  const int n = L.measStates;
+  double xs[6];
+#pragma unroll
+  for (int e = 0; e < 6; ++e) xs[e] = *wsPtr(P, L, n - 1, 6 + e);
+  float Pg[25];
+#pragma unroll
+  for (int e = 0; e < 25; ++e) Pg[e] = (e < 20 && e % 6 == 0) ? 1.f : 0.f; // rows 0..3: identity
+  for (int i = n - 2; i >= 0; --i) {
+    float Jn[25], G[25];
+#pragma unroll
+    for (int e = 0; e < 25; ++e) Jn[e] = (float)*wsPtr(P, L, i + 1, 12 + e);
+    invJacobian<float>(Jn, G);
+    bool nan = false;
+#pragma unroll
+    for (int e = 0; e < 25; ++e) nan = nan || (G[e] != G[e]);
+    if (nan) return false;
+    float dx[6];
+#pragma unroll
+    for (int e = 0; e < 6; ++e) dx[e] = (float)(xs[e] - *wsPtr(P, L, i + 1, e));
+    float y[6];
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+      if (r == 4) {
+        y[4] = dx[4];
+      } else {
+        const int gr = (r == 5) ? 4 : r;
+        float g = G[5 * gr] * dx[0];
+#pragma unroll
+        for (int k = 1; k < 5; ++k) g += G[5 * gr + k] * dx[k];
+        if (r == 5) g += dx[5];
+        y[r] = g;
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < 6; ++e) xs[e] = *wsPtr(P, L, i, 6 + e) + (double)y[e];
+    // Pg <- G Pg on the structure [[A, b, 0], [0, 1, 0], [c, d, 1]]
+    float Np[25];
+#pragma unroll
+    for (int r = 0; r < 5; ++r) {
+#pragma unroll
+      for (int c = 0; c < 5; ++c) {
+        float v = G[5 * r] * Pg[c];
+#pragma unroll
+        for (int k = 1; k < 4; ++k) v += G[5 * r + k] * Pg[5 * k + c];
+        if (c == 4) v += G[5 * r + 4];
+        if (r == 4) v += Pg[20 + c]; // row 5 of G times row 5 of Pg
+        Np[5 * r + c] = v;
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < 25; ++e) Pg[e] = Np[e];
+  }
+  // C_s(0) = Pg C Pg^T with C the last filtered covariance (in the stepper)
+  double Cs[21];
+  {
+    double M[6][6];
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        if (r == 4) {
+          M[r][c] = L.cov[sidx(4, c)];
+        } else {
+          const int gr = (r == 5) ? 4 : r;
+          double v = (double)Pg[5 * gr] * L.cov[sidx(0, c)];
+#pragma unroll
+          for (int k = 1; k < 5; ++k) v += (double)Pg[5 * gr + k] * L.cov[sidx(k, c)];
+          if (r == 5) v += L.cov[sidx(5, c)];
+          M[r][c] = v;
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+#pragma unroll
+      for (int c = r; c < 6; ++c) {
+        double v;
+        if (c == 4) {
+          v = M[r][4];
+        } else {
+          const int gc = (c == 5) ? 4 : c;
+          v = M[r][0] * (double)Pg[5 * gc];
+#pragma unroll
+          for (int k = 1; k < 5; ++k) v += M[r][k] * (double)Pg[5 * gc + k];
+          if (c == 5) v += M[r][5];
+        }
+        Cs[ut(r, c)] = v;
+      }
+    }
+  }
+  const PlaneD &pl = planes[L.firstPlane];
+  stepperUpdate(L, pl, xs, Cs, P.mass);
+  if (!P.faithful) planeJacToGlobal(L, pl);
+  L.navDir = -1;
+  ssInit(L, -1. * DBL_MAX);
+  L.pathAcc = 0.;
+  return true;
+}
+
 template <typename R>
 __device__ bool finalizeSmooth(Lane<R> &L, const Params &P, const PlaneD *planes) {
   L.smoothed = true;
+  if constexpr (sizeof(R) == sizeof(float)) {
+    if (!P.oSmoothed) return finalizeSmoothMixed(L, P, planes);
+  }
   const int n = L.measStates;
   double xs[6], Cs[21];
 #pragma unroll
@@ -1313,8 +1427,10 @@ template <typename R> __device__ void runEvent(Lane<R> &L, const Params &P, cons
 // EigenStepper::State from BoundParameters<LineSurface> (EigenStepper.hpp:40-61)
 // and the navigator initialisation; returns false for unusable input.
 template <typename R>
-__device__ void initLane(Lane<R> &L, const Params &P, const PlaneD *planes, int64_t i) {
+__device__ void initLane(Lane<R> &L, const Params &P, const PlaneD *planes, int64_t i,
+                         int64_t wsIdx) {
   L.idx = i;
+  L.wsIdx = wsIdx;
   L.pc = PC_DONE;
   L.parked = false;
   L.steps = 0;
@@ -1332,7 +1448,7 @@ __device__ void initLane(Lane<R> &L, const Params &P, const PlaneD *planes, int6
   L.result = true;
   L.tn = false;
   L.status = KF_TRACK_NOT_FITTED;
-  if (i >= P.n) return;
+  if (i < 0 || i >= P.n) return;
   double sp[6];
 #pragma unroll
   for (int e = 0; e < 6; ++e) sp[e] = P.start[(size_t)e * P.stride + i];

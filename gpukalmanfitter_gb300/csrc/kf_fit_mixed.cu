@@ -1,9 +1,12 @@
-// kf_fit_mixed.cu — instantiation of the fit kernel for the mixed form (FP32 propagation and Jacobians, FP64 Kalman algebra).
+// kf_fit_mixed.cu — mixed form (FP32 propagation and Jacobians, FP64 Kalman
+// algebra): grid kernel and the default persistent kernel.
 #include <cuda_runtime.h>
 
 #include "kf_kernels.cuh"
 
 cudaError_t launchFitMixed(const kfd::Params &P, unsigned grid, cudaStream_t s) {
-  kfd::fitKernel<kfd::kFitBlock, float><<<grid, kfd::kFitBlock, 0, s>>>(P);
+  kfd::fitGrid<kfd::kFitBlock, KF_MIN_BLOCKS_MIXED, float><<<grid, kfd::kFitBlock, 0, s>>>(P);
   return cudaGetLastError();
 }
+
+KF_PERSISTENT_LAUNCHER(launchPersistent_mixed_128_4, 128, 4, float)

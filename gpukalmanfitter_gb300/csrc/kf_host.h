@@ -1,0 +1,24 @@
+// kf_host.h — host-side helpers shared by the C ABI translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "kf_device.cuh"
+
+namespace kfh {
+
+char *errorBuffer(); // thread-local text behind kf_last_error_string()
+int32_t fail(int32_t code, const char *fmt, const char *detail = "");
+int32_t cudaFail(cudaError_t e, const char *where);
+
+// bytes of the per-state smoother workspace of n tracks
+size_t wsBytes(int64_t n, int32_t nSurf);
+// argument checks shared by every fit entry point
+int32_t checkCommon(const kf_inputs_t *in, const kf_config_t *cfg, const kf_geometry_t *geo,
+                    const kf_field_t *field);
+// kernel parameter block from the ABI structures
+void fillParams(kfd::Params &P, const kf_inputs_t *in, const kf_outputs_t *out,
+                const kf_config_t *cfg, const kf_geometry_t *geo, const kf_field_t *field,
+                void *ws);
+
+} // namespace kfh

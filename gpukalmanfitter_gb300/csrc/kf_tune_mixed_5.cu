@@ -1,0 +1,8 @@
+// kf_tune_mixed_5.cu — persistent kernel, mixed form, 128 threads per CTA and
+// at least 5 CTAs per SM (register budget 65536 / (128 x 5)): an autotuner
+// candidate.
+#include <cuda_runtime.h>
+
+#include "kf_kernels.cuh"
+
+KF_PERSISTENT_LAUNCHER(launchPersistent_mixed_128_5, 128, 5, float)

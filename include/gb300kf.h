@@ -102,9 +102,12 @@ typedef struct kf_config {
   int32_t faithful_jacobian; /* 1: keep the reference's jacToGlobal (not rebuilt
                                 after the update, EigenStepper.ipp:554-564);
                                 0: rebuild it at the updated state */
-  int32_t kernel;            /* kf_kernel_kind */
-  int32_t block_size;        /* threads per block; 0 = tuned default */
-  int32_t reserved0;
+  int32_t kernel;            /* kf_kernel_kind (informational; the entry point
+                                chooses the kernel) */
+  int32_t block_size;        /* batched form: threads per CTA, 0 = 128 */
+  int32_t min_blocks_per_sm; /* batched form: CTAs per SM the persistent kernel
+                                is compiled for (its register budget), 0 = 4;
+                                kf_autotune picks it */
 } kf_config_t;
 
 /* The surface sequence: boundless plane surfaces (PlaneSurface<InfiniteBounds>,
@@ -193,6 +196,44 @@ int32_t kf_fit_batch_host(const kf_inputs_t *host_in, kf_outputs_t *host_out,
                           const kf_config_t *cfg, const kf_geometry_t *geo,
                           const kf_field_t *field, void *device_staging,
                           size_t staging_bytes, void *stream);
+
+/* ---- batched form ---------------------------------------------------------
+ * Replaces the reference's one-thread-per-track launch
+ * (Run/GPU/Kernels.cu:6-45 from Run/GPU/KalmanFitterGPUTest.cu:461-472) for
+ * large batches with uneven track lengths, holes and outliers: tracks are
+ * ordered by expected work (sequence length, then |q/p|; longest first) by a
+ * counting sort on the device, and a persistent kernel (one resident grid,
+ * warps claiming 32 queue positions at a time) fits them.  Results are the
+ * same as kf_fit_batch's; the workspace is kf_batch_workspace_size bytes. */
+size_t kf_batch_workspace_size(const kf_config_t *cfg, int64_t n_tracks,
+                               int32_t n_surfaces);
+int32_t kf_fit_batch_sorted(const kf_inputs_t *in, kf_outputs_t *out,
+                            const kf_config_t *cfg, const kf_geometry_t *geo,
+                            const kf_field_t *field, void *workspace,
+                            size_t workspace_bytes, void *stream);
+
+/* A plan captures the whole batched pipeline (queue reset, sort, persistent
+ * fit) for fixed buffers into a CUDA graph; each launch replays it with one
+ * call.  `stream` must be a created stream (capture is not possible on the
+ * legacy default stream).  The buffers must outlive the plan. */
+typedef struct kf_batch_plan kf_batch_plan_t;
+int32_t kf_batch_plan_create(kf_batch_plan_t **plan, const kf_inputs_t *in,
+                             kf_outputs_t *out, const kf_config_t *cfg,
+                             const kf_geometry_t *geo, const kf_field_t *field,
+                             void *workspace, size_t workspace_bytes,
+                             void *stream);
+int32_t kf_batch_plan_launch(kf_batch_plan_t *plan, void *stream);
+void kf_batch_plan_destroy(kf_batch_plan_t *plan);
+
+/* Times every compiled persistent-kernel shape (CTAs per SM 2..5 at 128
+ * threads) of cfg->precision on the first 131072 tracks of the batch and
+ * returns the fastest configuration in *tuned (and its time per fit of the
+ * sample in *best_ms).  Overwrites the outputs of those tracks. */
+int32_t kf_autotune(const kf_inputs_t *in, kf_outputs_t *out,
+                    const kf_config_t *cfg, const kf_geometry_t *geo,
+                    const kf_field_t *field, void *workspace,
+                    size_t workspace_bytes, void *stream, kf_config_t *tuned,
+                    double *best_ms);
 
 /* ---- fitting without allocation ------------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc

@@ -1,0 +1,88 @@
+"""The batched form (length-sorted queue, persistent kernel, CUDA-graph plan,
+autotuner) gives exactly the per-track results of the one-thread-per-track
+kernel: the queue changes only which tracks share a warp, not any track's
+arithmetic."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+KEYS = ("params", "cov", "chi2", "status", "n_meas", "n_steps", "n_trials")
+
+
+def _same(a, b):
+    for k in KEYS:
+        assert np.array_equal(a[k], b[k]), k
+
+
+def _holes(kf, n, seed=11):
+    return kf.make_telescope(n, n_planes=30, x_first=50., x_step=50., min_len=5, max_len=30,
+                             hit_prob=0.9, outlier_prob=0.02, seed=seed)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_sorted_persistent_equals_grid(kf, precision):
+    tel = _holes(kf, 50_000)
+    cfg = kf.default_config(overstep_limit=0.1, outlier_chi2_cut=25.0, precision=precision)
+    b = kf.DeviceBatch(tel, cfg)
+    b.fit()
+    grid = b.results()
+    for v in b.out.values():
+        v.fill_(-7)
+    b.fit_sorted()
+    _same(b.results(), grid)
+
+
+def test_sorted_matches_oracle(kf, orc):
+    tel = _holes(kf, 5_000, seed=4)
+    cfg = kf.default_config(overstep_limit=0.1, outlier_chi2_cut=25.0)
+    b = kf.DeviceBatch(tel, cfg)
+    b.fit_sorted()
+    g = b.results()
+    o = orc.fit(tel, cfg, threads=0, variant="precise")
+    from conftest import parity_report
+    assert np.array_equal(g["status"], o["status"]) and np.array_equal(g["n_steps"], o["n_steps"])
+    rep = parity_report(g, o, 1e-9, mask=o["status"] == 0)
+    assert rep["params"] <= 1 and rep["chi2"] <= 1 and rep["cov"] <= 1, rep
+
+
+def test_graph_plan_replays(kf):
+    import torch
+    tel = _holes(kf, 20_000, seed=8)
+    cfg = kf.default_config(overstep_limit=0.1, outlier_chi2_cut=25.0, precision=1)
+    b = kf.DeviceBatch(tel, cfg)
+    b.fit()
+    ref = b.results()
+    s = torch.cuda.Stream()
+    b.make_plan(s)
+    for _ in range(2):
+        for v in b.out.values():
+            v.fill_(3)
+        b.launch_plan(s)
+        s.synchronize()
+        _same(b.results(), ref)
+    b.destroy_plan()
+
+
+def test_autotune_picks_a_compiled_shape(kf):
+    tel = _holes(kf, 40_000, seed=2)
+    cfg = kf.default_config(overstep_limit=0.1, outlier_chi2_cut=25.0)
+    b = kf.DeviceBatch(tel, cfg)
+    b.fit()
+    ref = b.results()
+    tuned, ms = b.autotune()
+    assert tuned.block_size == 128 and tuned.min_blocks_per_sm in (2, 3, 4, 5) and ms > 0
+    assert tuned.precision == cfg.precision and tuned.outlier_chi2_cut == 25.0
+    b.fit_sorted()
+    _same(b.results(), ref)
+
+
+@pytest.mark.parametrize("n", [1, 33, 4097])
+def test_sorted_small_batches(kf, n):
+    tel = kf.make_telescope(n, seed=n)
+    cfg = kf.default_config(overstep_limit=0.1)
+    b = kf.DeviceBatch(tel, cfg)
+    b.fit()
+    ref = b.results()
+    b.fit_sorted()
+    _same(b.results(), ref)
