@@ -1,13 +1,21 @@
 #!/usr/bin/env python3
 """Benchmark: fitted tracks/s of the GB300 Kalman fitter.
 
-Workload (plain FP64 fit at scale): 1M tracks per GPU through the 10-plane
+Headline workload (FP64 fit at scale): 1M tracks per GPU through the 10-plane
 telescope (x = 100..1000 mm, normal +x, no material) in a uniform 2 T field;
 pi+- with |p| in [1, 10] GeV, phi in +-0.1, theta in pi/2 +- 0.1; 50 um hits;
 seeds smeared by 50 um / 1 mrad / 5 %.  Synthetic, seeded, generated on the
-host.  One step = one fit of the whole batch (one kernel launch).
+host.  One step = one fit of the whole batch: in the batched form (default)
+one CUDA-graph launch (work-queue sort + persistent fit kernel, shape picked
+by the autotuner beforehand), in the plain form one grid kernel launch.  The
+line carries both forms on the same batch ("forms"), and a suite of two more
+one-GPU comparisons: 4M uneven tracks with holes and outliers on 30 planes,
+and 1M tracks on 30 planes in the FP32 field map (plain FP64 against batched
+FP64 and batched mixed precision).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--form batched|plain] [--workload W] [--precision fp64|mixed]
+                  [--tracks N] [--no-suite] [--no-e2e] [--no-cpu-baseline]
 
 The reference arm times the reference algorithm's CPU path (the C++ FP64
 restatement in oracle/, OpenMP over all host cores, the reference's -d cpu
@@ -167,6 +175,79 @@ def gpu_uuid() -> str | None:
         return None
 
 
+def param_diff(a: dict, b: dict) -> float:
+    """Largest |a - b| of the fitted parameters over max(|b|, sigma_b), over
+    the tracks both fitted."""
+    ok = (a["status"] == 0) & (b["status"] == 0)
+    if not ok.any():
+        return 0.0
+    sig = np.sqrt(np.abs(b["cov"][[0, 6, 11, 15, 18, 20]][:, ok]))
+    sc = np.maximum(np.abs(b["params"][:, ok]), sig)
+    sc = np.where(sc > 0, sc, 1.0)
+    return float(np.max(np.abs(a["params"][:, ok] - b["params"][:, ok]) / sc))
+
+
+def timed_steps(step, stream, steps: int, warmup: int, barrier) -> tuple:
+    """W untimed steps, then K steps between events on the launching stream,
+    bracketed by a barrier and a device synchronize on both sides.  Returns
+    (total ms, per-step ms list)."""
+    import torch
+    for _ in range(warmup):
+        step()
+    barrier()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(steps)]
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for a, b in evs:
+        a.record(stream)
+        step()
+        b.record(stream)
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    return t_start.elapsed_time(t_end), [a.elapsed_time(b) for a, b in evs]
+
+
+def batched_step(batch, stream) -> tuple:
+    """Autotune the persistent kernel shape on this batch, capture the sort and
+    the fit into a CUDA graph; one step = one graph launch (4 kernels)."""
+    tuned, tune_ms = batch.autotune(stream)
+    batch.make_plan(stream)
+    shape = {"threads_per_cta": tuned.block_size, "ctas_per_sm": tuned.min_blocks_per_sm,
+             "tracks_per_warp": 32, "autotune_best_ms_on_sample": round(tune_ms, 3)}
+    return (lambda: batch.launch_plan(stream)), 4, shape
+
+
+def suite_entry(kf, name: str, n: int, seed: int, stream, barrier, steps: int, warmup: int,
+                pairs) -> dict:
+    """Time the plain form (FP64 grid kernel) and the batched form of one
+    workload on the same inputs; pairs = [(label, precision), ...] batched."""
+    import torch
+    tel = make_workload(kf, name, n, seed)
+    out = {"workload": f"{name}: {WORKLOADS[name][0]}", "tracks": n}
+    with torch.cuda.stream(stream):
+        plain = kf.DeviceBatch(tel, fit_config(kf, name, "fp64"))
+    ms, _ = timed_steps(lambda: plain.fit(stream), stream, steps, warmup, barrier)
+    out["plain_fp64_tracks_per_s"] = n * steps / (ms * 1e-3)
+    out["plain_fp64_ms_per_step"] = ms / steps
+    del plain
+    for label, prec in pairs:
+        with torch.cuda.stream(stream):
+            b = kf.DeviceBatch(tel, fit_config(kf, name, prec))
+        step, _, shape = batched_step(b, stream)
+        ms, _ = timed_steps(step, stream, steps, warmup, barrier)
+        out[f"{label}_tracks_per_s"] = n * steps / (ms * 1e-3)
+        out[f"{label}_ms_per_step"] = ms / steps
+        out[f"{label}_shape"] = shape
+        out[f"{label}_vs_plain_fp64"] = out[f"{label}_tracks_per_s"] / out["plain_fp64_tracks_per_s"]
+        b.destroy_plan()
+        del b
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_gpu(args) -> None:
     import torch
     import gpukalmanfitter_gb300 as kf
@@ -183,44 +264,41 @@ def run_gpu(args) -> None:
     cfg = fit_config(kf, args.workload, args.precision)
     lib = kf.load()
 
-    stream = torch.cuda.Stream()
-    with torch.cuda.stream(stream):
-        batch = kf.DeviceBatch(tel, cfg)
-    torch.cuda.synchronize()
-    for _ in range(args.warmup):
-        batch.fit(stream)
-    torch.cuda.synchronize()
-
     def barrier():
         if dist is not None:
             dist.barrier()
         torch.cuda.synchronize()
 
-    # ---- kernel-resident timing: inputs in HBM, one launch per step
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-           for _ in range(args.steps)]
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        batch = kf.DeviceBatch(tel, cfg)
+    torch.cuda.synchronize()
+    shape = None
+    if args.form == "batched":
+        step, per_step, shape = batched_step(batch, stream)
+    else:
+        step, per_step = (lambda: batch.fit(stream)), 1
+
+    # ---- kernel-resident timing: inputs in HBM
     barrier()
     sampler = ClockSampler(gpu_uuid())
-    t_start = torch.cuda.Event(enable_timing=True)
-    t_end = torch.cuda.Event(enable_timing=True)
-    t_start.record(stream)
-    for a, b in evs:
-        a.record(stream)
-        batch.fit(stream)
-        b.record(stream)
-    t_end.record(stream)
-    torch.cuda.synchronize()
+    elapsed_ms, launch_ms = timed_steps(step, stream, args.steps, args.warmup, barrier)
     clocks = sampler.stop()
-    barrier()
-    elapsed_ms = t_start.elapsed_time(t_end)
-    launch_ms = [a.elapsed_time(b) for a, b in evs]
     if dist is not None:
         t = torch.tensor([elapsed_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         elapsed_ms = float(t.item())
     value = n * args.steps * world / (elapsed_ms * 1e-3)
-
     res = batch.results()
+
+    # the other form on the same batch (same precision): plain vs batched
+    forms = {args.form: value}
+    if args.form == "batched":
+        pms, _ = timed_steps(lambda: batch.fit(stream), stream, args.steps, args.warmup, barrier)
+        forms["plain"] = n * args.steps * world / (pms * 1e-3)
+        forms["max_param_diff_over_scale"] = param_diff(batch.results(), res)
+    batch.destroy_plan()
+
     ok_frac = float(np.mean(res["status"] == 0))
     flop = F.batch_flops(res["n_trials"], res["n_steps"], res["n_meas"], res["status"])
     dense_flop = F.batch_flops(res["n_trials"], res["n_steps"], res["n_meas"], res["status"], dense=True)
@@ -229,16 +307,30 @@ def run_gpu(args) -> None:
     rc = lib.kf_diag_fp64_fma_rate(C.c_int32(20000), C.byref(peak), C.c_void_p(stream.cuda_stream))
     peak_tflops = peak.value / 1e3 if rc == 0 else None
     achieved = flop / avg_launch_s / 1e12
-    traffic = None
-    tfile = ROOT / "profiles" / "traffic_fp64_fit.json"
-    if tfile.exists() and args.workload == "uniform10" and args.precision == "fp64":
-        try:
-            traffic = json.loads(tfile.read_text())["dram_bytes_per_track"] * n
-        except Exception:
-            traffic = None
+    traffic = traffic_estimate(args, n)
+    mb = F.batch_bytes(n, tel.n_surfaces)
+    hbm_peak, hbm_src = hbm_peak_gbs()
 
     # ---- end to end through the public host-buffer call (pinned memory)
-    e2e = None if args.no_e2e else run_e2e(kf, lib, tel, cfg, stream, args, barrier, dist)
+    e2e = None
+    if not args.no_e2e:
+        ecfg = fit_config(kf, args.workload, args.precision)
+        if args.form == "batched":
+            ecfg.kernel, ecfg.block_size = 2, shape["threads_per_cta"]
+            ecfg.min_blocks_per_sm = shape["ctas_per_sm"]
+        e2e = run_e2e(kf, lib, tel, ecfg, stream, args, barrier, dist)
+    del batch
+    torch.cuda.empty_cache()
+
+    suite = None
+    if not args.no_suite and world == 1:
+        # uneven tracks (4x the headline batch) and the field map (1x)
+        suite = {
+            "batching": suite_entry(kf, "holes30", 4 * n, 1234567892, stream, barrier, 3, 3,
+                                    [("batched_fp64", "fp64"), ("batched_mixed", "mixed")]),
+            "precision_map": suite_entry(kf, "map30", n, 1234567893, stream, barrier, 3, 3,
+                                         [("batched_mixed", "mixed"), ("batched_fp64", "fp64")]),
+        }
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -246,7 +338,6 @@ def run_gpu(args) -> None:
         cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
 
     if rank == 0:
-        mb = F.batch_bytes(n, tel.n_surfaces)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
@@ -254,27 +345,62 @@ def run_gpu(args) -> None:
             "dtype": "f64" if args.precision == "fp64" else "f32+f64",
             "data": "synthetic (seeded generator, analytic-helix truth)",
             "config": {**workload_config(args.workload, n, args.precision),
+                       "form": args.form, "kernel_shape": shape,
                        "parallelism": f"track shards, {world} GPU(s), no collective"},
+            "forms": forms,
             "fitted_fraction": ok_frac,
-            "gpu_launches": args.steps,
+            "gpu_launches": args.steps * per_step,
             "e2e": e2e,
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak_tflops,
                          "unit": "TFLOP/s", "frac": (achieved / peak_tflops) if peak_tflops else None,
                          "traffic": traffic,
-                         "peak_source": "measured in this run by kf_diag_fp64_fma_rate (independent DFMA chains on all SMs); "
-                                        "MEASURED_PEAKS.json lists only HBM and bf16 peaks",
+                         "peak_source": "measured in this run by kf_diag_fp64_fma_rate (independent "
+                                        "DFMA chains on all SMs); MEASURED_PEAKS.json is absent and "
+                                        "lists no FP64 peak",
                          "algorithmic_flop_per_launch": flop,
                          "algorithmic_flop_per_track": flop / n,
                          "dense_reference_flop_per_track": dense_flop / n,
-                         "algorithmic_bytes_per_launch": mb["total"],
-                         "avg_launch_ms": avg_launch_s * 1e3},
+                         "avg_launch_ms": avg_launch_s * 1e3,
+                         "launch_timed": "one step (graph of sort + fit kernels)" if args.form == "batched"
+                                         else "one fit kernel launch",
+                         "hbm_view": {"algorithmic_bytes_per_launch": mb["total"],
+                                      "achieved_gbs": mb["total"] / avg_launch_s / 1e9,
+                                      "peak_gbs": hbm_peak, "peak_source": hbm_src,
+                                      "frac": mb["total"] / avg_launch_s / 1e9 / hbm_peak}},
             "clocks": clocks,
         }
+        if suite is not None:
+            line["suite"] = suite
         if cpu is not None:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def traffic_estimate(args, n: int):
+    """DRAM bytes per launch from a committed ncu capture of the same kernel
+    and workload (scaled by tracks), or None."""
+    tfile = ROOT / "profiles" / "traffic.json"
+    if not tfile.exists():
+        return None
+    try:
+        rec = json.loads(tfile.read_text()).get(f"{args.workload}/{args.precision}/{args.form}")
+        return rec["dram_bytes_per_track"] * n if rec else None
+    except (ValueError, KeyError, TypeError):
+        return None
+
+
+def hbm_peak_gbs() -> tuple:
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        try:
+            v = json.loads(f.read_text()).get("hbm_gbs")
+            if v:
+                return float(v), "MEASURED_PEAKS.json hbm_gbs (measured)"
+        except ValueError:
+            pass
+    return 6800.0, "fallback 6.8 TB/s (MEASURED_PEAKS.json absent)"
 
 
 def run_e2e(kf, lib, tel, cfg, stream, args, barrier, dist) -> dict:
@@ -345,6 +471,11 @@ def main() -> None:
     ap.add_argument("--precision", default="fp64", choices=sorted(PRECISIONS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--form", default="batched", choices=["batched", "plain"],
+                    help="batched: sorted queue + persistent kernel in a CUDA graph; "
+                         "plain: one thread per track, grid over the batch")
+    ap.add_argument("--no-suite", action="store_true",
+                    help="skip the uneven-track and field-map comparisons")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

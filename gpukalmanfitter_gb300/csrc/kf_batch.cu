@@ -249,8 +249,10 @@ int32_t kf_autotune(const kf_inputs_t *in, kf_outputs_t *out, const kf_config_t 
                     const kf_geometry_t *geo, const kf_field_t *field, void *workspace,
                     size_t workspace_bytes, void *stream, kf_config_t *tuned, double *best_ms) {
   if (!in || !cfg || !tuned) return fail(KF_ERR_INVALID_ARGUMENT, "null argument%s");
+  // The first tracks (same stride) as the sample: at least several waves of
+  // the resident grid, so that the queue's tail does not decide the timing.
   kf_inputs_t sample = *in;
-  if (sample.n_tracks > 131072) sample.n_tracks = 131072; // first tracks, same stride
+  if (sample.n_tracks > 524288) sample.n_tracks = 524288;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   cudaEvent_t e0, e1;
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
@@ -265,22 +267,24 @@ int32_t kf_autotune(const kf_inputs_t *in, kf_outputs_t *out, const kf_config_t 
     c.block_size = v.bs;
     c.min_blocks_per_sm = v.minb;
     rc = kf_fit_batch_sorted(&sample, out, &c, geo, field, workspace, workspace_bytes, stream);
-    if (rc) break;
-    cudaEventRecord(e0, s);
-    for (int r = 0; r < 2 && rc == KF_SUCCESS; ++r)
+    // best of three timed runs after one warm-up
+    for (int r = 0; r < 3 && rc == KF_SUCCESS; ++r) {
+      cudaEventRecord(e0, s);
       rc = kf_fit_batch_sorted(&sample, out, &c, geo, field, workspace, workspace_bytes, stream);
-    cudaEventRecord(e1, s);
+      cudaEventRecord(e1, s);
+      if (rc) break;
+      if (cudaEventSynchronize(e1) != cudaSuccess) {
+        rc = cudaFail(cudaGetLastError(), "autotune timing");
+        break;
+      }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best) {
+        best = ms;
+        bestCfg = c;
+      }
+    }
     if (rc) break;
-    if (cudaEventSynchronize(e1) != cudaSuccess) {
-      rc = cudaFail(cudaGetLastError(), "autotune timing");
-      break;
-    }
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    if (ms / 2 < best) {
-      best = ms / 2;
-      bestCfg = c;
-    }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 
 #include "kf_host.h"
@@ -111,6 +112,14 @@ void fillParams(Params &P, const kf_inputs_t *in, const kf_outputs_t *out, const
     }
   }
   F.grid = reinterpret_cast<const float4 *>(field->grid);
+  for (int a = 0; a < 3; ++a) {
+    F.Bf[a] = (float)F.B[a];
+    F.mnf[a] = (float)F.mn[a];
+    F.invwf[a] = (float)F.invw[a];
+  }
+  F.scalef = (float)F.scale;
+  P.tolLoF = (float)(P.tol * 0.99);
+  P.tolHiF = (float)(P.tol * 1.01);
   for (int k = 0; k < in->n_surfaces; ++k) {
     PlaneD &pl = P.planes[k];
     for (int r = 0; r < 3; ++r) {
@@ -216,7 +225,8 @@ Staging stagingLayout(int64_t n, int32_t S, bool withSmoothed) {
   L.nsteps = take((size_t)n * 4);
   L.ntrials = take((size_t)n * 4);
   L.smoothed = withSmoothed ? take((size_t)S * 27 * n * 8) : 0;
-  L.ws = take(wsBytes(n, S));
+  // room for either form's workspace (the batched form adds its queue)
+  L.ws = take(std::max(wsBytes(n, S), kf_batch_workspace_size(nullptr, n, S)));
   L.total = o;
   return L;
 }
@@ -282,7 +292,10 @@ int32_t kf_fit_batch_host(const kf_inputs_t *hin, kf_outputs_t *hout, const kf_c
   dout.n_steps = reinterpret_cast<int32_t *>(d + L.nsteps);
   dout.n_trials = reinterpret_cast<int32_t *>(d + L.ntrials);
   dout.smoothed = sm ? reinterpret_cast<double *>(d + L.smoothed) : nullptr;
-  rc = kf_fit_batch(&din, &dout, cfg, geo, field, d + L.ws, wsBytes(n, S), stream);
+  const size_t wsb = std::max(wsBytes(n, S), kf_batch_workspace_size(nullptr, n, S));
+  rc = (cfg->kernel == KF_KERNEL_PERSISTENT)
+           ? kf_fit_batch_sorted(&din, &dout, cfg, geo, field, d + L.ws, wsb, stream)
+           : kf_fit_batch(&din, &dout, cfg, geo, field, d + L.ws, wsb, stream);
   if (rc) return rc;
   const size_t os = (size_t)hin->stride; // host outputs share the input stride
   chk(copyRows(hout->params, os, dout.params, n, 8, n, 6, cudaMemcpyDeviceToHost, s));

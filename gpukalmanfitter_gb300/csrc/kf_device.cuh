@@ -57,6 +57,7 @@ struct FieldD {
   double scale;
   double mn[3], invw[3];
   const float4 *grid;
+  float Bf[3], mnf[3], invwf[3], scalef; // FP32 copies for the mixed form
 };
 
 struct Params {
@@ -64,6 +65,7 @@ struct Params {
   int nSurf;
   int maxSteps, maxTrials, smoothing, faithful;
   double tol, cutoff, mass, overstep, surfTol, outlierCut;
+  float tolLoF, tolHiF; // mixed form: FP32 accept/reject band around tol
   const double *meas;
   const uint64_t *mask;
   const int32_t *nplanes;
@@ -144,16 +146,16 @@ __device__ __forceinline__ void getField(const FieldD &F, const double p[3], dou
 
 __device__ __forceinline__ void getField(const FieldD &F, const float p[3], float B[3]) {
   if (F.kind == KF_FIELD_CONSTANT) {
-    B[0] = (float)F.B[0];
-    B[1] = (float)F.B[1];
-    B[2] = (float)F.B[2];
+    B[0] = F.Bf[0];
+    B[1] = F.Bf[1];
+    B[2] = F.Bf[2];
     return;
   }
   int idx[3];
   float f[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    float g = (p[a] - (float)F.mn[a]) * (float)F.invw[a];
+    float g = (p[a] - F.mnf[a]) * F.invwf[a];
     int i = (int)floorf(g);
     i = min(max(i, 0), F.n[a] - 2);
     idx[a] = i;
@@ -165,7 +167,7 @@ __device__ __forceinline__ void getField(const FieldD &F, const float p[3], floa
   const float4 v010 = __ldg(F.grid + base + nx), v110 = __ldg(F.grid + base + nx + 1);
   const float4 v001 = __ldg(F.grid + base + nxy), v101 = __ldg(F.grid + base + nxy + 1);
   const float4 v011 = __ldg(F.grid + base + nxy + nx), v111 = __ldg(F.grid + base + nxy + nx + 1);
-  const float sc = (float)F.scale;
+  const float sc = F.scalef;
   auto tri = [&](float a000, float a100, float a010, float a110, float a001, float a101,
                  float a011, float a111) {
     float c00 = a000 + f[0] * (a100 - a000);
@@ -184,6 +186,27 @@ __device__ __forceinline__ void getField(const FieldD &F, const float p[3], floa
 // ---------------------------------------------------------------------------
 // Per-track state
 // ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------
+// Cold per-track state: the covariance and the jacToGlobal blocks are read
+// and written only at surface events (transport to a surface, filter,
+// smoother, final transport), never in the stepping loop.  They live in
+// dynamic shared memory, one column per thread ([element][thread]: a warp's
+// 32 lanes touch 32 consecutive words, no bank conflicts), so that the
+// stepping loop's register set stays small.  Every fit kernel runs
+// kLaneSlots threads per CTA.
+// ---------------------------------------------------------------------------
+constexpr int kLaneSlots = 128;
+template <typename R> struct ColdState {
+  double cov[21][kLaneSlots]; // bound covariance, upper triangle
+  R g03[12][kLaneSlots];      // jacToGlobal rows 0-2, cols 0-3
+  R g46[6][kLaneSlots];       // jacToGlobal rows 4-6, cols 2-3
+};
+extern __shared__ __align__(16) unsigned char kfColdSmem[];
+template <typename R> __device__ __forceinline__ ColdState<R> &coldState() {
+  return *reinterpret_cast<ColdState<R> *>(kfColdSmem);
+}
+template <typename R> constexpr size_t coldStateBytes() { return sizeof(ColdState<R>); }
+
 template <typename R> struct Lane {
   // ---- stepper state (EigenStepper::State)
   double pos[3], dir[3];
@@ -193,10 +216,12 @@ template <typename R> struct Lane {
   int ssDir;    // ConstrainedStep direction (+1 / -1)
   int navDir;
   R JA[3][3], Ja[3], Jb, JB[3][3], Jc[3]; // transport Jacobian blocks
-  R G03[3][4]; // jacToGlobal rows 0-2, cols 0-3
-  R G46[3][2]; // jacToGlobal rows 4-6, cols 2-3
-  R der[7];    // derivative rows 0..6 (row 7 is always 0)
-  double cov[21];
+  R k4[3];     // k4 of the last step (derivative rows 4..6)
+  bool stepped; // a step since the last Jacobian reset (else derivative = 0)
+  // cold state (shared memory, see ColdState)
+  __device__ __forceinline__ double &cov(int e) const { return coldState<R>().cov[e][threadIdx.x]; }
+  __device__ __forceinline__ R &g03(int r, int c) const { return coldState<R>().g03[r * 4 + c][threadIdx.x]; }
+  __device__ __forceinline__ R &g46(int r, int c) const { return coldState<R>().g46[r * 2 + c][threadIdx.x]; }
   // per-leg constants (functions of p only)
   double qop, dtds, d37;
   // ---- navigation / actor
@@ -287,8 +312,7 @@ template <typename R> __device__ __forceinline__ void resetTransport(Lane<R> &L)
     L.Jc[i] = R(0);
   }
   L.Jb = R(0);
-#pragma unroll
-  for (int i = 0; i < 7; ++i) L.der[i] = R(0);
+  L.stepped = false;
 }
 
 // PlaneSurface::initJacobianToGlobal (PlaneSurface.ipp:122-156)
@@ -299,17 +323,17 @@ template <typename R> __device__ __forceinline__ void planeJacToGlobal(Lane<R> &
   const R cosP = x * inv, sinP = y * inv;
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
-    L.G03[r][0] = (R)pl.U[r];
-    L.G03[r][1] = (R)pl.V[r];
-    L.G03[r][2] = R(0);
-    L.G03[r][3] = R(0);
+    L.g03(r, 0) = (R)pl.U[r];
+    L.g03(r, 1) = (R)pl.V[r];
+    L.g03(r, 2) = R(0);
+    L.g03(r, 3) = R(0);
   }
-  L.G46[0][0] = (-sinT) * sinP;
-  L.G46[0][1] = cosT * cosP;
-  L.G46[1][0] = sinT * cosP;
-  L.G46[1][1] = cosT * sinP;
-  L.G46[2][0] = R(0);
-  L.G46[2][1] = (-sinT);
+  L.g46(0, 0) = (-sinT) * sinP;
+  L.g46(0, 1) = cosT * cosP;
+  L.g46(1, 0) = sinT * cosP;
+  L.g46(1, 1) = cosT * sinP;
+  L.g46(2, 0) = R(0);
+  L.g46(2, 1) = (-sinT);
 }
 
 // LineSurface::referenceFrame (LineSurface.ipp:46-61), line axis z
@@ -498,7 +522,6 @@ template <typename R> __device__ void rkStep(Lane<R> &L, const Params &P) {
     }
     // propagationTime (EigenStepper.ipp:36-47)
     L.t += h * L.dtds;
-    L.der[3] = L.dtds;
     transportUpdate<double>(L, L.dir, L.qop, h, L.d37, s);
     // equations of motion
     const double hh6 = h * h / 6., h6 = h / 6.;
@@ -513,16 +536,13 @@ template <typename R> __device__ void rkStep(Lane<R> &L, const Params &P) {
     L.dir[1] *= inv;
     L.dir[2] *= inv;
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      L.der[i] = L.dir[i];
-      L.der[4 + i] = s.k4[i];
-    }
+    for (int i = 0; i < 3; ++i) L.k4[i] = s.k4[i];
   } else {
     // ---- mixed form: FP32 stages, transport and error estimate
     const float qopf = (float)L.qop;
     const float posf[3] = {(float)L.pos[0], (float)L.pos[1], (float)L.pos[2]};
     const float dirf[3] = {(float)L.dir[0], (float)L.dir[1], (float)L.dir[2]};
-    const float tolLo = (float)(P.tol * 0.99), tolHi = (float)(P.tol * 1.01);
+    const float tolLo = P.tolLoF, tolHi = P.tolHiF;
     RkStages<float> s;
     rkFirst<float>(P.field, posf, dirf, qopf, s);
     for (;;) {
@@ -573,12 +593,9 @@ template <typename R> __device__ void rkStep(Lane<R> &L, const Params &P) {
     L.dir[1] *= f;
     L.dir[2] *= f;
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      L.der[i] = (float)L.dir[i];
-      L.der[4 + i] = s.k4[i];
-    }
-    L.der[3] = (float)L.dtds;
+    for (int i = 0; i < 3; ++i) L.k4[i] = s.k4[i];
   }
+  L.stepped = true;
   L.pathAcc += h;
   L.rkSteps++;
 }
@@ -599,14 +616,14 @@ template <typename R>
 __device__ __forceinline__ void applyTransport(const Lane<R> &L, Transported<R> &X) {
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
-    X.Pt[r][0] = L.G03[r][0];
-    X.Pt[r][1] = L.G03[r][1];
+    X.Pt[r][0] = L.g03(r, 0);
+    X.Pt[r][1] = L.g03(r, 1);
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
-      X.Pt[r][2 + c] = L.G03[r][2 + c] + L.JA[r][0] * L.G46[0][c] +
-                       L.JA[r][1] * L.G46[1][c] + L.JA[r][2] * L.G46[2][c];
-      X.Dd[r][2 + c] = L.JB[r][0] * L.G46[0][c] + L.JB[r][1] * L.G46[1][c] +
-                       L.JB[r][2] * L.G46[2][c];
+      X.Pt[r][2 + c] = L.g03(r, 2 + c) + L.JA[r][0] * L.g46(0, c) +
+                       L.JA[r][1] * L.g46(1, c) + L.JA[r][2] * L.g46(2, c);
+      X.Dd[r][2 + c] = L.JB[r][0] * L.g46(0, c) + L.JB[r][1] * L.g46(1, c) +
+                       L.JB[r][2] * L.g46(2, c);
     }
     X.Pt[r][4] = L.Ja[r];
     X.Dd[r][0] = R(0);
@@ -627,14 +644,23 @@ __device__ __forceinline__ void applyTransport(const Lane<R> &L, Transported<R> 
 template <typename R>
 __device__ __forceinline__ void projectCov(Lane<R> &L, Transported<R> &X, const R sVec[5],
                                            const R ax0[3], const R ax1[3], double Jst[25]) {
+  // derivative (EigenStepper.ipp:320-325): direction, dt/ds and k4 of the
+  // last step; zero right after a Jacobian reset
+  R der[7];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    der[r] = L.stepped ? (R)L.dir[r] : R(0);
+    der[4 + r] = L.stepped ? L.k4[r] : R(0);
+  }
+  der[3] = L.stepped ? (R)L.dtds : R(0);
 #pragma unroll
   for (int c = 0; c < 5; ++c) {
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
-      X.Pt[r][c] -= L.der[r] * sVec[c];
-      X.Dd[r][c] -= L.der[4 + r] * sVec[c];
+      X.Pt[r][c] -= der[r] * sVec[c];
+      X.Dd[r][c] -= der[4 + r] * sVec[c];
     }
-    X.R3[c] -= L.der[3] * sVec[c];
+    X.R3[c] -= der[3] * sVec[c];
   }
   const R x = (R)L.dir[0], y = (R)L.dir[1], z = (R)L.dir[2];
   const R cosT = z, sinT = sqrt(x * x + y * y);
@@ -661,12 +687,12 @@ __device__ __forceinline__ void projectCov(Lane<R> &L, Transported<R> &X, const 
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
       if (i == 4) {
-        M[i][j] = L.cov[sidx(4, j)];
+        M[i][j] = L.cov(sidx(4, j));
       } else {
-        double s = J[i][0] * L.cov[sidx(0, j)];
+        double s = J[i][0] * L.cov(sidx(0, j));
 #pragma unroll
-        for (int k = 1; k < 5; ++k) s += J[i][k] * L.cov[sidx(k, j)];
-        if (i == 5) s += L.cov[sidx(5, j)];
+        for (int k = 1; k < 5; ++k) s += J[i][k] * L.cov(sidx(k, j));
+        if (i == 5) s += L.cov(sidx(5, j));
         M[i][j] = s;
       }
     }
@@ -685,7 +711,7 @@ __device__ __forceinline__ void projectCov(Lane<R> &L, Transported<R> &X, const 
         for (int k = 1; k < 5; ++k) s += M[i][k] * J[j][k];
         if (j == 5) s += M[i][5];
       }
-      L.cov[ut(i, j)] = s;
+      L.cov(ut(i, j)) = s;
     }
   }
 #pragma unroll
@@ -795,7 +821,7 @@ __device__ __forceinline__ void stepperUpdate(Lane<R> &L, const PlaneD &pl, cons
   L.p = fabs(1. / par[4]);
   L.t = par[5];
 #pragma unroll
-  for (int e = 0; e < 21; ++e) L.cov[e] = cov[e];
+  for (int e = 0; e < 21; ++e) L.cov(e) = cov[e];
   legConstants(L, mass);
 }
 
@@ -822,8 +848,8 @@ __device__ void filterHit(Lane<R> &L, const Params &P, const PlaneD *planes, int
   const double *mp = P.meas + (size_t)k * 5 * P.stride + L.idx;
   const double m0 = mp[0], m1 = mp[P.stride], v00 = mp[2 * P.stride],
                v01 = mp[3 * P.stride], v11 = mp[4 * P.stride];
-  const double S00 = L.cov[0] + v00, S01 = L.cov[1] + v01, S10 = L.cov[1] + v01,
-               S11 = L.cov[6] + v11;
+  const double S00 = L.cov(0) + v00, S01 = L.cov(1) + v01, S10 = L.cov(1) + v01,
+               S11 = L.cov(6) + v11;
   const double det = S00 * S11 - S01 * S10;
   const double i00 = S11 / det, i01 = -S01 / det, i10 = -S10 / det, i11 = S00 / det;
   const double r0 = m0 - pred[0], r1 = m1 - pred[1];
@@ -844,7 +870,7 @@ __device__ void filterHit(Lane<R> &L, const Params &P, const PlaneD *planes, int
     double K0[6], K1[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
-      const double c0 = L.cov[sidx(i, 0)], c1 = L.cov[sidx(i, 1)];
+      const double c0 = L.cov(sidx(i, 0)), c1 = L.cov(sidx(i, 1));
       K0[i] = c0 * i00 + c1 * i10;
       K1[i] = c0 * i01 + c1 * i11;
     }
@@ -856,7 +882,7 @@ __device__ void filterHit(Lane<R> &L, const Params &P, const PlaneD *planes, int
       for (int i = 0; i < 6; ++i) {
 #pragma unroll
         for (int j = i; j < 6; ++j)
-          cf[ut(i, j)] = L.cov[ut(i, j)] - K0[i] * L.cov[sidx(0, j)] - K1[i] * L.cov[sidx(1, j)];
+          cf[ut(i, j)] = L.cov(ut(i, j)) - K0[i] * L.cov(sidx(0, j)) - K1[i] * L.cov(sidx(1, j));
       }
     } else {
       // Joseph form with H = [I2 0]:
@@ -871,10 +897,10 @@ __device__ void filterHit(Lane<R> &L, const Params &P, const PlaneD *planes, int
       for (int i = 0; i < 6; ++i) {
 #pragma unroll
         for (int j = i; j < 6; ++j) {
-          const double ka = K0[i] * L.cov[sidx(0, j)] + K1[i] * L.cov[sidx(1, j)];
-          const double ak = K0[j] * L.cov[sidx(0, i)] + K1[j] * L.cov[sidx(1, i)];
+          const double ka = K0[i] * L.cov(sidx(0, j)) + K1[i] * L.cov(sidx(1, j));
+          const double ak = K0[j] * L.cov(sidx(0, i)) + K1[j] * L.cov(sidx(1, i));
           const double ksk = KS0[i] * K0[j] + KS1[i] * K1[j];
-          cf[ut(i, j)] = (L.cov[ut(i, j)] - ka) - (ak - ksk);
+          cf[ut(i, j)] = (L.cov(ut(i, j)) - ka) - (ak - ksk);
         }
       }
     }
@@ -1034,13 +1060,13 @@ __device__ bool finalizeSmoothMixed(Lane<R> &L, const Params &P, const PlaneD *p
 #pragma unroll
       for (int c = 0; c < 6; ++c) {
         if (r == 4) {
-          M[r][c] = L.cov[sidx(4, c)];
+          M[r][c] = L.cov(sidx(4, c));
         } else {
           const int gr = (r == 5) ? 4 : r;
-          double v = (double)Pg[5 * gr] * L.cov[sidx(0, c)];
+          double v = (double)Pg[5 * gr] * L.cov(sidx(0, c));
 #pragma unroll
-          for (int k = 1; k < 5; ++k) v += (double)Pg[5 * gr + k] * L.cov[sidx(k, c)];
-          if (r == 5) v += L.cov[sidx(5, c)];
+          for (int k = 1; k < 5; ++k) v += (double)Pg[5 * gr + k] * L.cov(sidx(k, c));
+          if (r == 5) v += L.cov(sidx(5, c));
           M[r][c] = v;
         }
       }
@@ -1084,7 +1110,7 @@ __device__ bool finalizeSmooth(Lane<R> &L, const Params &P, const PlaneD *planes
   for (int e = 0; e < 6; ++e) xs[e] = *wsPtr(P, L, n - 1, 6 + e);
   // the stepper holds the last filtered covariance
 #pragma unroll
-  for (int e = 0; e < 21; ++e) Cs[e] = L.cov[e];
+  for (int e = 0; e < 21; ++e) Cs[e] = L.cov(e);
   if (P.oSmoothed) {
 #pragma unroll
     for (int e = 0; e < 6; ++e)
@@ -1298,7 +1324,7 @@ __device__ bool actor(Lane<R> &L, const Params &P, const PlaneD *planes, bool he
 #pragma unroll
       for (int e = 0; e < 6; ++e) P.oParams[(size_t)e * P.stride + L.idx] = out[e];
 #pragma unroll
-      for (int e = 0; e < 21; ++e) P.oCov[(size_t)e * P.stride + L.idx] = L.cov[e];
+      for (int e = 0; e < 21; ++e) P.oCov[(size_t)e * P.stride + L.idx] = L.cov(e);
       L.finished = true;
     }
   }
@@ -1493,7 +1519,7 @@ __device__ void initLane(Lane<R> &L, const Params &P, const PlaneD *planes, int6
   L.pathAcc = 0.;
   resetTransport(L);
 #pragma unroll
-  for (int e = 0; e < 21; ++e) L.cov[e] = P.scov[(size_t)e * P.stride + i];
+  for (int e = 0; e < 21; ++e) L.cov(e) = P.scov[(size_t)e * P.stride + i];
   legConstants(L, P.mass);
   // LineSurface::initJacobianToGlobal (LineSurface.ipp:63-112)
   {
@@ -1522,12 +1548,12 @@ __device__ void initLane(Lane<R> &L, const Params &P, const PlaneD *planes, int6
     for (int r = 0; r < 3; ++r) {
       dP[r] = dP[r] - xp * X[r];
       dT[r] = dT[r] - xt * X[r];
-      L.G03[r][0] = (R)X[r];
-      L.G03[r][1] = (R)Y[r];
-      L.G03[r][2] = (R)(dP[r] * sp[0] * ipdn);
-      L.G03[r][3] = (R)(dT[r] * sp[0] * ipdn);
-      L.G46[r][0] = (R)G46[r][0];
-      L.G46[r][1] = (R)G46[r][1];
+      L.g03(r, 0) = (R)X[r];
+      L.g03(r, 1) = (R)Y[r];
+      L.g03(r, 2) = (R)(dP[r] * sp[0] * ipdn);
+      L.g03(r, 3) = (R)(dT[r] * sp[0] * ipdn);
+      L.g46(r, 0) = (R)G46[r][0];
+      L.g46(r, 1) = (R)G46[r][1];
     }
   }
   L.pc = PC_PRE;

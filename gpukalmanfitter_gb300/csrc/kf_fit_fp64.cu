@@ -5,7 +5,7 @@
 #include "kf_kernels.cuh"
 
 cudaError_t launchFitFp64(const kfd::Params &P, unsigned grid, cudaStream_t s) {
-  kfd::fitGrid<kfd::kFitBlock, KF_MIN_BLOCKS_FP64, double><<<grid, kfd::kFitBlock, 0, s>>>(P);
+  kfd::fitGrid<kfd::kFitBlock, KF_MIN_BLOCKS_FP64, double><<<grid, kfd::kFitBlock, kfd::coldStateBytes<double>(), s>>>(P);
   return cudaGetLastError();
 }
 

@@ -5,7 +5,7 @@
 #include "kf_kernels.cuh"
 
 cudaError_t launchFitMixed(const kfd::Params &P, unsigned grid, cudaStream_t s) {
-  kfd::fitGrid<kfd::kFitBlock, KF_MIN_BLOCKS_MIXED, float><<<grid, kfd::kFitBlock, 0, s>>>(P);
+  kfd::fitGrid<kfd::kFitBlock, KF_MIN_BLOCKS_MIXED, float><<<grid, kfd::kFitBlock, kfd::coldStateBytes<float>(), s>>>(P);
   return cudaGetLastError();
 }
 

@@ -16,7 +16,7 @@
 
 namespace kfd {
 
-constexpr int kFitBlock = 128; // threads per CTA of the grid form
+constexpr int kFitBlock = kLaneSlots; // threads per CTA of every fit kernel
 #ifndef KF_MIN_BLOCKS_FP64
 #define KF_MIN_BLOCKS_FP64 4
 #endif
@@ -54,8 +54,14 @@ __device__ __forceinline__ void fitWarp(const Params &P, const PlaneD *sp, int64
   }
 }
 
+// Static shared memory (surface table) plus the dynamic cold state must stay
+// within the 48 KB a CTA gets without an opt-in.
+static_assert(sizeof(PlaneD) * KF_MAX_PLANES + sizeof(ColdState<double>) <= 48 * 1024,
+              "fit kernel shared memory above 48 KB");
+
 template <int BS, int MINB, typename R>
 __global__ void __launch_bounds__(BS, MINB) fitGrid(const __grid_constant__ Params P) {
+  static_assert(BS == kLaneSlots, "cold state holds kLaneSlots columns");
   __shared__ PlaneD sp[KF_MAX_PLANES];
   for (int k = threadIdx.x; k < P.nSurf; k += BS) sp[k] = P.planes[k];
   __syncthreads();
@@ -65,6 +71,7 @@ __global__ void __launch_bounds__(BS, MINB) fitGrid(const __grid_constant__ Para
 
 template <int BS, int MINB, typename R>
 __global__ void __launch_bounds__(BS, MINB) fitPersistent(const __grid_constant__ Params P) {
+  static_assert(BS == kLaneSlots, "cold state holds kLaneSlots columns");
   __shared__ PlaneD sp[KF_MAX_PLANES];
   for (int k = threadIdx.x; k < P.nSurf; k += BS) sp[k] = P.planes[k];
   __syncthreads();
@@ -92,12 +99,12 @@ __global__ void __launch_bounds__(BS, MINB) fitPersistent(const __grid_constant_
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);                   \
     if (e != cudaSuccess) return e;                                                          \
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kfd::fitPersistent<BS, MINB, R>, \
-                                                      BS, 0);                                \
+                                                      BS, kfd::coldStateBytes<R>());         \
     if (e != cudaSuccess) return e;                                                          \
     int64_t blocks = (int64_t)sms * (per > 0 ? per : 1);                                     \
     const int64_t need = (P.n + BS - 1) / BS;                                                \
     if (blocks > need) blocks = need;                                                        \
     if (blocks < 1) blocks = 1;                                                              \
-    kfd::fitPersistent<BS, MINB, R><<<(unsigned)blocks, BS, 0, s>>>(P);                      \
+    kfd::fitPersistent<BS, MINB, R><<<(unsigned)blocks, BS, kfd::coldStateBytes<R>(), s>>>(P); \
     return cudaGetLastError();                                                               \
   }

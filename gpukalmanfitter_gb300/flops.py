@@ -49,6 +49,6 @@ def batch_bytes(n_tracks: int, n_surfaces: int) -> dict:
     once, smoother states written and read back once."""
     inputs = n_tracks * (n_surfaces * 5 * 8 + 8 + 4 + 6 * 8 + 21 * 8 + 3 * 8)
     outputs = n_tracks * (6 * 8 + 21 * 8 + 8 + 4 * 4)
-    workspace = 2 * n_tracks * n_surfaces * 79 * 8
+    workspace = 2 * n_tracks * n_surfaces * 37 * 8  # stored states (kStateStride doubles)
     return {"inputs": inputs, "outputs": outputs, "workspace": workspace,
             "total": inputs + outputs + workspace}

@@ -102,8 +102,10 @@ typedef struct kf_config {
   int32_t faithful_jacobian; /* 1: keep the reference's jacToGlobal (not rebuilt
                                 after the update, EigenStepper.ipp:554-564);
                                 0: rebuild it at the updated state */
-  int32_t kernel;            /* kf_kernel_kind (informational; the entry point
-                                chooses the kernel) */
+  int32_t kernel;            /* kf_kernel_kind: kf_fit_batch_host runs the batched
+                                form for KF_KERNEL_PERSISTENT and the
+                                thread-per-track grid otherwise; the device-buffer
+                                entry points each run their own form */
   int32_t block_size;        /* batched form: threads per CTA, 0 = 128 */
   int32_t min_blocks_per_sm; /* batched form: CTAs per SM the persistent kernel
                                 is compiled for (its register budget), 0 = 4;
@@ -226,9 +228,11 @@ int32_t kf_batch_plan_launch(kf_batch_plan_t *plan, void *stream);
 void kf_batch_plan_destroy(kf_batch_plan_t *plan);
 
 /* Times every compiled persistent-kernel shape (CTAs per SM 2..5 at 128
- * threads) of cfg->precision on the first 131072 tracks of the batch and
- * returns the fastest configuration in *tuned (and its time per fit of the
- * sample in *best_ms).  Overwrites the outputs of those tracks. */
+ * threads) of cfg->precision on the first min(n, 524288) tracks of the batch
+ * (best of three runs after a warm-up) and returns the fastest configuration
+ * in *tuned (and its time per fit of the sample in *best_ms).  Overwrites
+ * the outputs of those tracks.  Shapes differ in register allocation only;
+ * results agree to rounding (not bitwise) across shapes. */
 int32_t kf_autotune(const kf_inputs_t *in, kf_outputs_t *out,
                     const kf_config_t *cfg, const kf_geometry_t *geo,
                     const kf_field_t *field, void *workspace,

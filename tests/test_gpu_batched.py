@@ -74,7 +74,34 @@ def test_autotune_picks_a_compiled_shape(kf):
     assert tuned.block_size == 128 and tuned.min_blocks_per_sm in (2, 3, 4, 5) and ms > 0
     assert tuned.precision == cfg.precision and tuned.outlier_chi2_cut == 25.0
     b.fit_sorted()
-    _same(b.results(), ref)
+    g = b.results()
+    # other register budgets may contract or order FP64 operations differently:
+    # equal step sequences and results to rounding
+    assert np.array_equal(g["status"], ref["status"]) and np.array_equal(g["n_steps"], ref["n_steps"])
+    from conftest import parity_report
+    rep = parity_report(g, ref, 1e-10, mask=ref["status"] == 0)
+    assert rep["params"] <= 1 and rep["chi2"] <= 1 and rep["cov"] <= 1, rep
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("minb", [2, 3, 4, 5])
+def test_every_compiled_shape_runs(kf, precision, minb):
+    tel = _holes(kf, 8_000, seed=minb)
+    cfg = kf.default_config(overstep_limit=0.1, outlier_chi2_cut=25.0, precision=precision,
+                            min_blocks_per_sm=minb, block_size=128)
+    b = kf.DeviceBatch(tel, cfg)
+    b.fit()
+    ref = b.results()
+    b.fit_sorted()
+    g = b.results()
+    assert np.array_equal(g["status"], ref["status"])
+    assert np.mean(g["n_steps"] == ref["n_steps"]) > 0.999
+    ok = (ref["status"] == 0) & (g["n_steps"] == ref["n_steps"])
+    from conftest import parity_report
+    # mixed: FP32 rounding differs between register budgets as it differs from
+    # FP64 (up to ~1e-4 of sigma on d0), so only a coarse bound applies
+    rep = parity_report(g, ref, 1e-10 if precision == 0 else 1e-3, mask=ok)
+    assert rep["params"] <= 1 and rep["chi2"] <= 1, rep
 
 
 @pytest.mark.parametrize("n", [1, 33, 4097])
