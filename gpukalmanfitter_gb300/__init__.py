@@ -24,12 +24,12 @@ from . import build as _build
 __all__ = [
     "load", "KfConfig", "KfGeometry", "KfField", "KfInputs", "KfOutputs", "SynthConfig",
     "default_config", "Telescope", "make_telescope", "fit_device", "fit_host",
-    "TRACK_STATUS", "KfError",
+    "TRACK_STATUS", "KfError", "AdjointBatch", "align_geometry",
 ]
 
 KF_MAX_PLANES = 64
 TRACK_STATUS = {0: "ok", 1: "meas_mismatch", 2: "smoother_nan", 3: "max_steps",
-                4: "no_hits", 5: "bad_input", 6: "not_fitted"}
+                4: "no_hits", 5: "bad_input", 6: "not_fitted", 7: "adjoint_failed"}
 TESLA = 0.000299792458  # GeV/(e*mm)
 
 
@@ -130,6 +130,16 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.kf_autotune.restype = C.c_int32
     lib.kf_autotune.argtypes = lib.kf_fit_batch.argtypes + [C.POINTER(KfConfig),
                                                             C.POINTER(C.c_double)]
+    lib.kf_fit_batch_noalloc.restype = C.c_int32
+    lib.kf_noalloc_scratch_bytes.restype = C.c_size_t
+    lib.kf_noalloc_last_error_string.restype = C.c_char_p
+    lib.kf_diag_fp64_fma_rate.restype = C.c_int32
+    lib.kf_adjoint_workspace_size.restype = C.c_size_t
+    lib.kf_adjoint_workspace_size.argtypes = [C.POINTER(KfConfig), C.c_int64, C.c_int32]
+    lib.kf_adjoint_batch.restype = C.c_int32
+    lib.kf_adjoint_batch.argtypes = [C.POINTER(KfInputs), C.c_void_p, C.POINTER(KfConfig),
+                                     C.POINTER(KfGeometry), C.POINTER(KfField), C.c_int32,
+                                     C.c_void_p, C.c_size_t, C.c_void_p]
     lib.kf_synth_config_default.argtypes = [C.POINTER(SynthConfig)]
     lib.kf_synth_geometry.restype = C.c_int32
     lib.kf_synth_field_map.restype = C.c_int32
@@ -422,3 +432,97 @@ def fit_device(tel: Telescope, cfg: KfConfig | None = None, **kw) -> dict:
     b = DeviceBatch(tel, cfg, **kw)
     b.fit()
     return b.results()
+
+
+# ---------------------------------------------------------------------------
+# chi2 adjoint (kf_adjoint_batch)
+# ---------------------------------------------------------------------------
+class KfAdjointOutputs(C.Structure):
+    _fields_ = [("chi2", C.c_void_p), ("status", C.c_void_p), ("grad_start", C.c_void_p),
+                ("grad_align", C.c_void_p), ("grad_field_scale", C.c_void_p),
+                ("chi2_total", C.c_void_p)]
+
+
+def _rot(a: np.ndarray) -> np.ndarray:
+    """R = Rx(wx) Ry(wy) Rz(wz) for a = (wx, wy, wz) (the same composition as
+    the alignment frame rotation of the adjoint's tests)."""
+    cx, sx, cy, sy, cz, sz = np.cos(a[0]), np.sin(a[0]), np.cos(a[1]), np.sin(a[1]), np.cos(a[2]), np.sin(a[2])
+    rx = np.array([[1, 0, 0], [0, cx, -sx], [0, sx, cx]])
+    ry = np.array([[cy, 0, sy], [0, 1, 0], [-sy, 0, cy]])
+    rz = np.array([[cz, -sz, 0], [sz, cz, 0], [0, 0, 1]])
+    return rx @ ry @ rz
+
+
+def align_geometry(center: np.ndarray, rotation: np.ndarray, alignment: np.ndarray):
+    """Plane centres shifted by alignment[:, 0:3] and frames (U, V, T columns of
+    rotation[k].reshape(3, 3)) rotated by alignment[:, 3:6] about the global axes."""
+    c = np.array(center, dtype=np.float64).reshape(-1, 3) + alignment[:, :3]
+    r = np.array(rotation, dtype=np.float64).reshape(-1, 3, 3).copy()
+    for k in range(r.shape[0]):
+        r[k] = _rot(alignment[k, 3:]) @ r[k]
+    return c, r.reshape(-1, 9)
+
+
+def rotation_increment_jacobian(a: np.ndarray) -> np.ndarray:
+    """E with (incremental global rotation vector) = E d(wx, wy, wz) for
+    R = Rx(wx) Ry(wy) Rz(wz): columns e_x, Rx e_y, Rx Ry e_z."""
+    cx, sx, cy, sy = np.cos(a[0]), np.sin(a[0]), np.cos(a[1]), np.sin(a[1])
+    rx = np.array([[1, 0, 0], [0, cx, -sx], [0, sx, cx]])
+    ry = np.array([[cy, 0, sy], [0, 1, 0], [-sy, 0, cy]])
+    return np.stack([np.array([1., 0., 0.]), rx @ np.array([0., 1., 0.]),
+                     rx @ ry @ np.array([0., 0., 1.])], axis=1)
+
+
+class AdjointBatch:
+    """d(total smoothed chi2) / d(plane alignment, start parameters, field
+    scale) of a batch on the device (kf_adjoint_batch)."""
+
+    def __init__(self, tel: Telescope, cfg: KfConfig | None = None, device: str = "cuda"):
+        import torch
+        self.tel = tel
+        self.cfg = cfg or default_config()
+        n, S = tel.n, tel.n_surfaces
+        t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)
+        self.arrays = {k: (t(v) if v is not None else None) for k, v in tel_arrays(tel, True).items()}
+        self.out = {"chi2": torch.zeros(n, dtype=torch.float64, device=device),
+                    "status": torch.zeros(n, dtype=torch.int32, device=device),
+                    "grad_start": torch.zeros((6, n), dtype=torch.float64, device=device),
+                    "grad_align": torch.zeros((S, 6), dtype=torch.float64, device=device),
+                    "grad_field_scale": torch.zeros(1, dtype=torch.float64, device=device),
+                    "chi2_total": torch.zeros(1, dtype=torch.float64, device=device)}
+        self.aout = KfAdjointOutputs(*[self.out[k].data_ptr() for k in
+                                       ("chi2", "status", "grad_start", "grad_align",
+                                        "grad_field_scale", "chi2_total")])
+        lib = load()
+        self.ws_bytes = int(lib.kf_adjoint_workspace_size(C.byref(self.cfg), n, S))
+        if n > 0 and self.ws_bytes < n * S * 37 * 8:
+            raise KfError(f"implausible adjoint workspace size {self.ws_bytes}")
+        self.ws = torch.empty(max(self.ws_bytes, 1), dtype=torch.uint8, device=device)
+        self.ins = inputs_struct(self.arrays, n, S, lambda x: x.data_ptr())
+        self.center = np.array(tel.center, dtype=np.float64)
+        self.rotation = np.array(tel.rotation, dtype=np.float64)
+
+    def run(self, grad: bool = True, alignment: np.ndarray | None = None,
+            field_scale: float = 1.0, stream=None) -> dict:
+        """One call; alignment (S, 6) perturbs the geometry first (the gradient
+        is then taken at that geometry, with respect to incremental alignment)."""
+        import torch
+        s = stream if stream is not None else torch.cuda.current_stream()
+        if alignment is None:
+            c, r = self.center, self.rotation
+        else:
+            c, r = align_geometry(self.center, self.rotation, np.asarray(alignment, np.float64))
+        c = np.ascontiguousarray(c, dtype=np.float64)
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        geo = KfGeometry(self.tel.n_surfaces, 0, _ptr(c), _ptr(r))
+        field = self.tel.field(scale=field_scale)
+        _check(load().kf_adjoint_batch(C.byref(self.ins), C.byref(self.aout), C.byref(self.cfg),
+                                       C.byref(geo), C.byref(field), C.c_int32(1 if grad else 0),
+                                       C.c_void_p(self.ws.data_ptr()), C.c_size_t(self.ws_bytes),
+                                       C.c_void_p(s.cuda_stream)))
+        s.synchronize()
+        return {k: v.cpu().numpy() for k, v in self.out.items()}
+
+    def set_start(self, start: np.ndarray) -> None:
+        import torch
+        self.arrays["start"].copy_(torch.from_numpy(np.ascontiguousarray(start, np.float64)))

@@ -207,7 +207,18 @@ template <typename R> __device__ __forceinline__ ColdState<R> &coldState() {
 }
 template <typename R> constexpr size_t coldStateBytes() { return sizeof(ColdState<R>); }
 
-template <typename R> struct Lane {
+// Recording hook of a lane: the fit kernels use NoHook (every call compiles
+// to nothing); the chi2 adjoint records its tape through these calls.
+struct NoHook {
+  template <class LT> __device__ __forceinline__ void stepBegin(const LT &) {}
+  template <class LT> __device__ __forceinline__ void trial(const LT &, double) {}
+  template <class LT> __device__ __forceinline__ void stepEnd(const LT &, bool) {}
+  template <class LT> __device__ __forceinline__ void actorSet(const LT &, int) {}
+  template <class LT> __device__ __forceinline__ void hitBegin(const LT &, int) {}
+  __device__ __forceinline__ void hitEnd(bool) {}
+};
+
+template <typename R, typename H = NoHook> struct Lane {
   // ---- stepper state (EigenStepper::State)
   double pos[3], dir[3];
   double p, q, t;
@@ -234,6 +245,7 @@ template <typename R> struct Lane {
   double perigee[3];
   int64_t idx;   // track index (inputs and outputs)
   int64_t wsIdx; // workspace column (queue position in the batched form)
+  H hook;
 };
 
 // ---- ConstrainedStep (ConstrainedStep.hpp:22-108) --------------------------
@@ -247,7 +259,7 @@ __device__ __forceinline__ long long okey(double x) {
 __device__ __forceinline__ long long akey(double x) {
   return __double_as_longlong(x) & 0x7fffffffffffffffLL;
 }
-template <typename R> __device__ __forceinline__ double ssMax(const Lane<R> &L) {
+template <typename R, typename H> __device__ __forceinline__ double ssMax(const Lane<R, H> &L) {
   double m = L.ss[0];
   long long km = okey(m);
 #pragma unroll
@@ -260,7 +272,7 @@ template <typename R> __device__ __forceinline__ double ssMax(const Lane<R> &L) 
   }
   return m;
 }
-template <typename R> __device__ __forceinline__ double ssMin(const Lane<R> &L) {
+template <typename R, typename H> __device__ __forceinline__ double ssMin(const Lane<R, H> &L) {
   double m = L.ss[0];
   long long km = okey(m);
 #pragma unroll
@@ -273,18 +285,18 @@ template <typename R> __device__ __forceinline__ double ssMin(const Lane<R> &L) 
   }
   return m;
 }
-template <typename R> __device__ __forceinline__ double ssValue(const Lane<R> &L) {
+template <typename R, typename H> __device__ __forceinline__ double ssValue(const Lane<R, H> &L) {
   return L.ssDir == 1 ? ssMin(L) : ssMax(L);
 }
-template <typename R> __device__ __forceinline__ void ssRelease(Lane<R> &L, int t) {
+template <typename R, typename H> __device__ __forceinline__ void ssRelease(Lane<R, H> &L, int t) {
   L.ss[t] = (L.ssDir == 1) ? ssMax(L) : ssMin(L);
 }
-template <typename R> __device__ __forceinline__ void ssUpdate(Lane<R> &L, double v, int t, bool rel) {
+template <typename R, typename H> __device__ __forceinline__ void ssUpdate(Lane<R, H> &L, double v, int t, bool rel) {
   if (rel) ssRelease(L, t);
   const double c = L.ss[t];
   L.ss[t] = akey(c) < akey(v) ? c : v;
 }
-template <typename R> __device__ __forceinline__ void ssInit(Lane<R> &L, double value) {
+template <typename R, typename H> __device__ __forceinline__ void ssInit(Lane<R, H> &L, double value) {
   L.ssDir = value > 0. ? 1 : -1;
   L.ss[0] = DBL_MAX * L.ssDir;
   L.ss[1] = DBL_MAX * L.ssDir;
@@ -293,14 +305,14 @@ template <typename R> __device__ __forceinline__ void ssInit(Lane<R> &L, double 
 }
 
 // per-leg constants: q/p, dt/ds and the dt/d(q/p) coefficient
-template <typename R> __device__ __forceinline__ void legConstants(Lane<R> &L, double mass) {
+template <typename R, typename H> __device__ __forceinline__ void legConstants(Lane<R, H> &L, double mass) {
   L.qop = L.q / L.p;
   L.dtds = hypot(1., mass / L.p);
   L.d37 = mass * mass * L.q / (L.p * L.dtds);
 }
 
 // ---- Jacobian resets -------------------------------------------------------
-template <typename R> __device__ __forceinline__ void resetTransport(Lane<R> &L) {
+template <typename R, typename H> __device__ __forceinline__ void resetTransport(Lane<R, H> &L) {
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
 #pragma unroll
@@ -316,7 +328,7 @@ template <typename R> __device__ __forceinline__ void resetTransport(Lane<R> &L)
 }
 
 // PlaneSurface::initJacobianToGlobal (PlaneSurface.ipp:122-156)
-template <typename R> __device__ __forceinline__ void planeJacToGlobal(Lane<R> &L, const PlaneD &pl) {
+template <typename R, typename H> __device__ __forceinline__ void planeJacToGlobal(Lane<R, H> &L, const PlaneD &pl) {
   const R x = (R)L.dir[0], y = (R)L.dir[1], z = (R)L.dir[2];
   const R cosT = z, sinT = sqrt(x * x + y * y);
   const R inv = R(1) / sinT;
@@ -407,8 +419,8 @@ __device__ __forceinline__ T rkTrial(const FieldD &F, const T pos[3], const T di
 
 // transportMatrix (EigenStepper.ipp:50-124) on its non-zero blocks and
 // jacTransport = D * jacTransport (EigenStepper.ipp:312-318)
-template <typename R>
-__device__ __forceinline__ void transportUpdate(Lane<R> &L, const R dir[3], R qop, R h, R d37,
+template <typename R, typename H>
+__device__ __forceinline__ void transportUpdate(Lane<R, H> &L, const R dir[3], R qop, R h, R d37,
                                                 const RkStages<R> &s) {
   const R half_h = h * R(0.5);
   R dk1dL[3], dk2dL[3], dk3dL[3], dk4dL[3], tmp[3], c[3], cc[3];
@@ -500,15 +512,17 @@ __device__ __forceinline__ void transportUpdate(Lane<R> &L, const R dir[3], R qo
   L.Jb = L.Jb + D37;
 }
 
-template <typename R> __device__ void rkStep(Lane<R> &L, const Params &P) {
+template <typename R, typename H> __device__ void rkStep(Lane<R, H> &L, const Params &P) {
   long nTrials = 0;
   double h = ssValue(L);
   if constexpr (sizeof(R) == sizeof(double)) {
     // ---- plain form: FP64 throughout
     RkStages<double> s;
     rkFirst<double>(P.field, L.pos, L.dir, L.qop, s);
+    L.hook.stepBegin(L);
     for (;;) {
       L.rkTrials++;
+      L.hook.trial(L, h);
       const double err = rkTrial<double>(P.field, L.pos, L.dir, L.qop, h, s);
       if (err <= P.tol) break;
       const double scale = smin(smax(0.25, pow(P.tol / fabs(2. * err), 0.25)), 4.);
@@ -516,10 +530,13 @@ template <typename R> __device__ void rkStep(Lane<R> &L, const Params &P) {
       L.ss[kAccuracy] = hn;
       L.ssDir = hn > 0. ? 1 : -1;
       h = ssValue(L);
-      if (h * h < P.cutoff * P.cutoff) return;
-      if (nTrials > P.maxTrials) return;
+      if (h * h < P.cutoff * P.cutoff || nTrials > P.maxTrials) {
+        L.hook.stepEnd(L, false);
+        return;
+      }
       nTrials++;
     }
+    L.hook.stepEnd(L, true);
     // propagationTime (EigenStepper.ipp:36-47)
     L.t += h * L.dtds;
     transportUpdate<double>(L, L.dir, L.qop, h, L.d37, s);
@@ -612,8 +629,8 @@ template <typename R> struct Transported {
   R Pt[3][5], R3[5], Dd[3][5];
 };
 
-template <typename R>
-__device__ __forceinline__ void applyTransport(const Lane<R> &L, Transported<R> &X) {
+template <typename R, typename H>
+__device__ __forceinline__ void applyTransport(const Lane<R, H> &L, Transported<R> &X) {
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
     X.Pt[r][0] = L.g03(r, 0);
@@ -641,8 +658,8 @@ __device__ __forceinline__ void applyTransport(const Lane<R> &L, Transported<R> 
 // and cov <- J cov J^T (in FP64).  ax0/ax1 are the surface's local axes
 // (rows 0 and 1 of jacToLocal); the direction rows follow
 // PlaneSurface.ipp:158-189 / LineSurface.ipp:114-143.
-template <typename R>
-__device__ __forceinline__ void projectCov(Lane<R> &L, Transported<R> &X, const R sVec[5],
+template <typename R, typename H>
+__device__ __forceinline__ void projectCov(Lane<R, H> &L, Transported<R> &X, const R sVec[5],
                                            const R ax0[3], const R ax1[3], double Jst[25]) {
   // derivative (EigenStepper.ipp:320-325): direction, dt/ds and k4 of the
   // last step; zero right after a Jacobian reset
@@ -726,8 +743,8 @@ __device__ __forceinline__ void projectCov(Lane<R> &L, Transported<R> &X, const 
 
 // BoundParameters from the free state (CovarianceEngine.hpp:363-370 and
 // coordinate_transformations.hpp:115-128): angles and q/p from the momentum.
-template <typename R>
-__device__ __forceinline__ void boundAngles(const Lane<R> &L, double out[6], double mom[3]) {
+template <typename R, typename H>
+__device__ __forceinline__ void boundAngles(const Lane<R, H> &L, double out[6], double mom[3]) {
   const double qopF = L.q / L.p;
   const double pabs = fabs(1. / qopF);
   mom[0] = pabs * L.dir[0];
@@ -743,8 +760,8 @@ __device__ __forceinline__ void boundAngles(const Lane<R> &L, double out[6], dou
 }
 
 // boundState<PlaneSurface> (EigenStepper.ipp:516-540) incl. re-initialisation
-template <typename R>
-__device__ void boundStatePlane(Lane<R> &L, const PlaneD &pl, double out[6], double Jst[25]) {
+template <typename R, typename H>
+__device__ void boundStatePlane(Lane<R, H> &L, const PlaneD &pl, double out[6], double Jst[25]) {
   Transported<R> X;
   applyTransport(L, X);
   // PlaneSurface::derivativeFactors (PlaneSurface.ipp:191-204)
@@ -768,8 +785,8 @@ __device__ void boundStatePlane(Lane<R> &L, const PlaneD &pl, double out[6], dou
 }
 
 // boundState<LineSurface> towards the perigee line (axis z through `c`)
-template <typename R>
-__device__ void boundStateLine(Lane<R> &L, const double c[3], double out[6]) {
+template <typename R, typename H>
+__device__ void boundStateLine(Lane<R, H> &L, const double c[3], double out[6]) {
   Transported<R> X;
   applyTransport(L, X);
   double mX[3], mY[3], mD[3];
@@ -805,8 +822,8 @@ __device__ void boundStateLine(Lane<R> &L, const double c[3], double out[6]) {
 
 // EigenStepper::update (EigenStepper.ipp:554-564) from bound parameters on a
 // plane (boundParameters2freeParameters, coordinate_transformations.hpp:145-158)
-template <typename R>
-__device__ __forceinline__ void stepperUpdate(Lane<R> &L, const PlaneD &pl, const double par[6],
+template <typename R, typename H>
+__device__ __forceinline__ void stepperUpdate(Lane<R, H> &L, const PlaneD &pl, const double par[6],
                                               const double cov[21], double mass) {
 #pragma unroll
   for (int r = 0; r < 3; ++r) L.pos[r] = pl.U[r] * par[0] + pl.V[r] * par[1] + pl.c[r];
@@ -828,8 +845,8 @@ __device__ __forceinline__ void stepperUpdate(Lane<R> &L, const PlaneD &pl, cons
 // ---------------------------------------------------------------------------
 // Workspace access: state s of track i, element e
 // ---------------------------------------------------------------------------
-template <typename R>
-__device__ __forceinline__ double *wsPtr(const Params &P, const Lane<R> &L, int s, int e) {
+template <typename R, typename H>
+__device__ __forceinline__ double *wsPtr(const Params &P, const Lane<R, H> &L, int s, int e) {
   return P.ws + ((size_t)s * kStateStride + e) * (size_t)P.wsStride + L.wsIdx;
 }
 
@@ -840,9 +857,10 @@ __device__ __forceinline__ double *wsPtr(const Params &P, const Lane<R> &L, int 
 // (I - KH) C (I - KH)^T + K V K^T, which stays positive definite when the
 // predicted covariance carries FP32-level errors from the Jacobian.
 // ---------------------------------------------------------------------------
-template <typename R>
-__device__ void filterHit(Lane<R> &L, const Params &P, const PlaneD *planes, int k) {
+template <typename R, typename H>
+__device__ void filterHit(Lane<R, H> &L, const Params &P, const PlaneD *planes, int k) {
   const PlaneD &pl = planes[k];
+  L.hook.hitBegin(L, k);
   double pred[6], Jst[25];
   boundStatePlane(L, pl, pred, Jst);
   const double *mp = P.meas + (size_t)k * 5 * P.stride + L.idx;
@@ -910,6 +928,7 @@ __device__ void filterHit(Lane<R> &L, const Params &P, const PlaneD *planes, int
     stepperUpdate(L, pl, filt, cf, P.mass);
     if (!P.faithful) planeJacToGlobal(L, pl);
   }
+  L.hook.hitEnd(outlier);
   L.measStates++;
 }
 
@@ -996,8 +1015,8 @@ __device__ __forceinline__ void invJacobian(const T J[25], T Gi[25]) {
 // added to the FP64 filtered parameters; the smoothed covariance is needed at
 // the first state only, C_s(0) = Pg C_f(n-1) Pg^T with Pg = G_1 ... G_{n-1}
 // accumulated in FP32 on the Jacobian structure.
-template <typename R>
-__device__ bool finalizeSmoothMixed(Lane<R> &L, const Params &P, const PlaneD *planes) {
+template <typename R, typename H>
+__device__ bool finalizeSmoothMixed(Lane<R, H> &L, const Params &P, const PlaneD *planes) {
   L.smoothed = true;
   const int n = L.measStates;
   double xs[6];
@@ -1098,8 +1117,8 @@ __device__ bool finalizeSmoothMixed(Lane<R> &L, const Params &P, const PlaneD *p
   return true;
 }
 
-template <typename R>
-__device__ bool finalizeSmooth(Lane<R> &L, const Params &P, const PlaneD *planes) {
+template <typename R, typename H>
+__device__ bool finalizeSmooth(Lane<R, H> &L, const Params &P, const PlaneD *planes) {
   L.smoothed = true;
   if constexpr (sizeof(R) == sizeof(float)) {
     if (!P.oSmoothed) return finalizeSmoothMixed(L, P, planes);
@@ -1205,8 +1224,9 @@ __device__ bool finalizeSmooth(Lane<R> &L, const Params &P, const PlaneD *planes
 // ---------------------------------------------------------------------------
 // Navigation (DirectNavigator.hpp:158-225, SteppingHelper.hpp:31-65)
 // ---------------------------------------------------------------------------
-template <typename R>
-__device__ __forceinline__ int updateSurfaceStatus(Lane<R> &L, const Params &P, const PlaneD &pl) {
+template <typename R, typename H>
+__device__ __forceinline__ int updateSurfaceStatus(Lane<R, H> &L, const Params &P, const PlaneD &pl,
+                                                   int k) {
   const double d0 = L.navDir * L.dir[0], d1 = L.navDir * L.dir[1], d2 = L.navDir * L.dir[2];
   const double denom = d0 * pl.T[0] + d1 * pl.T[1] + d2 * pl.T[2];
   if (denom != 0.0) {
@@ -1221,17 +1241,18 @@ __device__ __forceinline__ int updateSurfaceStatus(Lane<R> &L, const Params &P, 
     const double oLimit = -P.overstep;
     if (path > oLimit && path * path < pLimit * pLimit) {
       ssUpdate(L, L.navDir * path, kActor, true);
+      L.hook.actorSet(L, k);
       return kReachable;
     }
   }
   return kMissed;
 }
 
-template <typename R>
-__device__ __forceinline__ void navStatus(Lane<R> &L, const Params &P, const PlaneD *planes) {
+template <typename R, typename H>
+__device__ __forceinline__ void navStatus(Lane<R, H> &L, const Params &P, const PlaneD *planes) {
   L.current = -1;
   if (L.next != L.nSeq) {
-    if (updateSurfaceStatus(L, P, planes[L.next]) == kOnSurface) {
+    if (updateSurfaceStatus(L, P, planes[L.next], L.next) == kOnSurface) {
       L.current = L.next;
       ++L.next;
       if (L.next != L.nSeq) ssRelease(L, kActor);
@@ -1239,19 +1260,19 @@ __device__ __forceinline__ void navStatus(Lane<R> &L, const Params &P, const Pla
   }
 }
 
-template <typename R>
-__device__ __forceinline__ void navTarget(Lane<R> &L, const Params &P, const PlaneD *planes) {
+template <typename R, typename H>
+__device__ __forceinline__ void navTarget(Lane<R, H> &L, const Params &P, const PlaneD *planes) {
   L.current = -1;
   if (L.next != L.nSeq) {
-    if (updateSurfaceStatus(L, P, planes[L.next]) == kMissed) ++L.next;
+    if (updateSurfaceStatus(L, P, planes[L.next], L.next) == kMissed) ++L.next;
   } else {
     L.navBreak = true;
   }
 }
 
 // LineSurface::intersect (LineSurface.ipp:229-262) along navDir * dir
-template <typename R>
-__device__ __forceinline__ void lineIntersect(const Lane<R> &L, const Params &P, double &u,
+template <typename R, typename H>
+__device__ __forceinline__ void lineIntersect(const Lane<R, H> &L, const Params &P, double &u,
                                               int &status) {
   const double ea0 = L.navDir * L.dir[0], ea1 = L.navDir * L.dir[1], ea2 = L.navDir * L.dir[2];
   const double m0 = L.perigee[0] - L.pos[0], m1 = L.perigee[1] - L.pos[1],
@@ -1272,8 +1293,8 @@ __device__ __forceinline__ void lineIntersect(const Lane<R> &L, const Params &P,
 // runs when no filter update, smoothing or final transport is due, and
 // returns false without touching the state otherwise.
 // ---------------------------------------------------------------------------
-template <typename R>
-__device__ bool actor(Lane<R> &L, const Params &P, const PlaneD *planes, bool heavy) {
+template <typename R, typename H>
+__device__ bool actor(Lane<R, H> &L, const Params &P, const PlaneD *planes, bool heavy) {
   const bool onPlane = L.current >= 0 && !L.smoothed && !L.finished;
   const bool hit = onPlane && ((L.mask >> L.current) & 1ull);
   if (!heavy) {
@@ -1333,7 +1354,7 @@ __device__ bool actor(Lane<R> &L, const Params &P, const PlaneD *planes, bool he
 
 // Kalman aborter (KalmanFitter.hpp:682-694) then PathLimitReached
 // (StandardAborters.hpp:37-56)
-template <typename R> __device__ __forceinline__ bool aborters(Lane<R> &L, const Params &P) {
+template <typename R, typename H> __device__ __forceinline__ bool aborters(Lane<R, H> &L, const Params &P) {
   if (!L.result || L.finished) return true;
   if (L.targetReached) return true;
   const double distance = L.navDir * fabs(DBL_MAX) - L.pathAcc;
@@ -1343,7 +1364,7 @@ template <typename R> __device__ __forceinline__ bool aborters(Lane<R> &L, const
   return limit;
 }
 
-template <typename R> __device__ __forceinline__ void finish(Lane<R> &L, const Params &P) {
+template <typename R, typename H> __device__ __forceinline__ void finish(Lane<R, H> &L, const Params &P) {
   int st;
   if (!L.result)
     st = L.smoothed ? KF_TRACK_SMOOTHER_NAN : KF_TRACK_MEAS_MISMATCH;
@@ -1364,7 +1385,7 @@ template <typename R> __device__ __forceinline__ void finish(Lane<R> &L, const P
 // (heavy actor work) is due, or the track is done; runEvent() executes the
 // pending actor call with heavy work allowed and continues.
 // ---------------------------------------------------------------------------
-template <typename R> __device__ void advance(Lane<R> &L, const Params &P, const PlaneD *planes) {
+template <typename R, typename H> __device__ void advance(Lane<R, H> &L, const Params &P, const PlaneD *planes) {
   for (;;) {
     switch (L.pc) {
     case PC_PRE:
@@ -1417,7 +1438,7 @@ template <typename R> __device__ void advance(Lane<R> &L, const Params &P, const
   }
 }
 
-template <typename R> __device__ void runEvent(Lane<R> &L, const Params &P, const PlaneD *planes) {
+template <typename R, typename H> __device__ void runEvent(Lane<R, H> &L, const Params &P, const PlaneD *planes) {
   L.parked = false;
   switch (L.pc) {
   case PC_PRE:
@@ -1452,8 +1473,8 @@ template <typename R> __device__ void runEvent(Lane<R> &L, const Params &P, cons
 
 // EigenStepper::State from BoundParameters<LineSurface> (EigenStepper.hpp:40-61)
 // and the navigator initialisation; returns false for unusable input.
-template <typename R>
-__device__ void initLane(Lane<R> &L, const Params &P, const PlaneD *planes, int64_t i,
+template <typename R, typename H>
+__device__ void initLane(Lane<R, H> &L, const Params &P, const PlaneD *planes, int64_t i,
                          int64_t wsIdx) {
   L.idx = i;
   L.wsIdx = wsIdx;

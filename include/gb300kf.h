@@ -66,7 +66,9 @@ enum kf_track_status {
   KF_TRACK_MAX_STEPS = 3,     /* propagation hit maxSteps without the aborter */
   KF_TRACK_NO_HITS = 4,       /* no measurement on the track */
   KF_TRACK_BAD_INPUT = 5,     /* q/p == 0 or non-finite start parameters */
-  KF_TRACK_NOT_FITTED = 6     /* target surface never reached */
+  KF_TRACK_NOT_FITTED = 6,    /* target surface never reached */
+  KF_TRACK_ADJOINT_FAILED = 7 /* kf_adjoint_batch: a step failed or the
+                                 segment tape was full; no gradient */
 };
 
 enum kf_precision {
@@ -261,6 +263,38 @@ int32_t kf_fit_batch_noalloc(const kf_inputs_t *in, kf_outputs_t *out,
                              const kf_field_t *field, void *stream);
 size_t kf_noalloc_scratch_bytes(void);
 const char *kf_noalloc_last_error_string(void);
+
+/* ---- chi2 adjoint ---------------------------------------------------------
+ * No counterpart in the reference (it has no derivatives).  Objective: the
+ * total smoothed chi2, sum over tracks with status KF_TRACK_OK and their
+ * non-outlier measurement states of (m - H x_s)^T V^-1 (m - H x_s), x_s the
+ * smoothed parameters of the same fit as kf_fit_batch.  Gradients by a
+ * hand-written reverse sweep (FP64) with respect to
+ *   - the alignment of each plane: centre shift (dx, dy, dz) in mm and small
+ *     rotations (wx, wy, wz) in rad about the global axes applied to the
+ *     plane frame, at the geometry given (zero alignment);
+ *   - each track's start parameters (perigee d0, z0, phi, theta, q/p, t);
+ *   - the field scale (kf_field_t.scale).
+ * Supported: cfg->precision FP64, uniform field, faithful_jacobian = 1.
+ * The forward states are checkpointed every 5 measurement states and each
+ * segment is recomputed during the reverse sweep. */
+typedef struct kf_adjoint_outputs {
+  double *chi2;             /* [n] smoothed chi2 per track (0 unless OK) */
+  int32_t *status;          /* [n] kf_track_status */
+  double *grad_start;       /* [6][stride] d chi2_track / d start parameter, or NULL */
+  double *grad_align;       /* [n_surfaces][6] d chi2_total / d alignment, or NULL */
+  double *grad_field_scale; /* [1] d chi2_total / d field scale, or NULL */
+  double *chi2_total;       /* [1] total chi2, or NULL */
+} kf_adjoint_outputs_t;
+
+size_t kf_adjoint_workspace_size(const kf_config_t *cfg, int64_t n_tracks, int32_t n_surfaces);
+
+/* compute_gradient = 0 runs the forward part only (chi2, status), the
+ * function the gradient differentiates, for finite-difference checks. */
+int32_t kf_adjoint_batch(const kf_inputs_t *in, kf_adjoint_outputs_t *out,
+                         const kf_config_t *cfg, const kf_geometry_t *geo,
+                         const kf_field_t *field, int32_t compute_gradient, void *workspace,
+                         size_t workspace_bytes, void *stream);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,175 @@
+"""The chi2 adjoint (kf_adjoint_batch) against central finite differences of
+its own forward, against finite differences of the FP64 oracle's smoothed
+chi2 (the reference-forward gradient), and through torch.autograd.gradcheck.
+
+Workload: a 20-plane telescope (x = 50..1000 mm) in a uniform 2 T field with
+planes misaligned by N(0, 100 um) shifts and N(0, 1 mrad) rotations in the
+truth geometry; the fit uses the nominal geometry."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TEL = dict(n_planes=20, x_first=50., x_step=50., mis_shift=0.1, mis_rot=1e-3)
+
+
+@pytest.fixture(scope="module")
+def ab(kf):
+    tel = kf.make_telescope(2000, seed=4242, **TEL)
+    b = kf.AdjointBatch(tel, kf.default_config(overstep_limit=0.1))
+    return b
+
+
+def chi2_from_smoothed(kf, tel, sm, status):
+    """sum over states of (m - xs)^T V^-1 (m - xs); every plane has a hit here"""
+    S = tel.n_surfaces
+    out = np.zeros(tel.n)
+    for s in range(S):
+        m0, m1, v00, v01, v11 = tel.meas[s]
+        r0 = m0 - sm[s, 0]
+        r1 = m1 - sm[s, 1]
+        det = v00 * v11 - v01 * v01
+        out += (r0 * (v11 * r0 - v01 * r1) + r1 * (v00 * r1 - v01 * r0)) / det
+    return np.where(status == 0, out, 0.0)
+
+
+def test_forward_chi2_is_the_fits_smoothed_chi2(kf, ab):
+    r = ab.run(grad=False)
+    assert np.mean(r["status"] == 0) > 0.99
+    b = kf.DeviceBatch(ab.tel, ab.cfg, smoothed=True)
+    b.fit()
+    g = b.results()
+    assert np.array_equal(g["status"], r["status"])
+    ref = chi2_from_smoothed(kf, ab.tel, g["smoothed"], g["status"])
+    ok = r["status"] == 0
+    assert np.max(np.abs(r["chi2"][ok] - ref[ok]) / ref[ok]) < 1e-10
+    assert abs(r["chi2_total"][0] - r["chi2"].sum()) <= 1e-9 * r["chi2_total"][0]
+
+
+def _rel(a, b, scale):
+    return np.abs(a - b) / np.maximum(np.abs(b), scale)
+
+
+# Finite differences: the fourth-order central stencil
+#   f'(x) ~ (f(x-2h) - 8 f(x-h) + 8 f(x+h) - f(x+2h)) / 12h
+# with h = 1e-4 of each parameter's scale.  At a step of 1e-6 relative the
+# differences of the FP64 forward carry rounding noise of ~1e-5 relative per
+# track (the error falls as 1/h down to the truncation floor), so the check
+# is made where the differences themselves are accurate to ~1e-8.
+def _fd4(f, h):
+    return (f(-2 * h) - 8 * f(-h) + 8 * f(h) - f(2 * h)) / (12 * h)
+
+
+START_SCALE = np.array([0.05, 0.05, 1e-3, 1e-3, 0.05, 1.0])  # mm, mm, rad, rad, 1/GeV, ns
+ALIGN_SCALE = np.array([0.1] * 3 + [1e-3] * 3)              # mm, rad
+
+
+def test_start_gradient_matches_finite_differences(kf, ab):
+    r = ab.run(grad=True)
+    ok = r["status"] == 0
+    g = r["grad_start"]
+    start0 = ab.tel.start.copy()
+    for e in range(6):
+        h = 1e-4 * np.maximum(np.abs(start0[e]), START_SCALE[e])
+
+        def f(d):
+            sp = start0.copy()
+            sp[e] += d
+            ab.set_start(sp)
+            return ab.run(grad=False)["chi2"]
+
+        fd = _fd4(f, h)
+        if e == 5:  # no time measurement: chi2 does not depend on t
+            assert np.all(g[e] == 0.) and np.max(np.abs(fd)) < 1e-6
+            continue
+        rel = _rel(g[e][ok], fd[ok], np.median(np.abs(fd[ok])))
+        assert np.median(rel) < 3e-7 and np.quantile(rel, 0.99) < 3e-6, (e, np.sort(rel)[-4:])
+        assert abs(g[e][ok].sum() - fd[ok].sum()) <= 1e-6 * np.abs(fd[ok]).sum()
+    ab.set_start(start0)
+
+
+def test_alignment_gradient_matches_finite_differences(ab):
+    r = ab.run(grad=True)
+    ga = r["grad_align"]
+    rels = []
+    for k in range(ab.tel.n_surfaces):
+        for a in range(6):
+            def f(d):
+                al = np.zeros((ab.tel.n_surfaces, 6))
+                al[k, a] = d
+                return ab.run(grad=False, alignment=al)["chi2_total"][0]
+            fd = _fd4(f, 1e-4 * ALIGN_SCALE[a])
+            rels.append(abs(ga[k, a] - fd) / max(abs(fd), 1e-3 * np.max(np.abs(ga[:, a]))))
+    rels = np.array(rels)
+    assert np.median(rels) < 1e-7 and np.max(rels) < 1e-6, np.sort(rels)[-5:]
+
+
+def test_field_scale_gradient_matches_finite_differences(ab):
+    r = ab.run(grad=True)
+    fd = _fd4(lambda d: ab.run(grad=False, field_scale=1 + d)["chi2_total"][0], 1e-5)
+    assert abs(r["grad_field_scale"][0] - fd) <= 1e-6 * abs(fd)
+
+
+def test_reference_forward_gradient(kf, orc):
+    """Central differences of the oracle's smoothed chi2 (the reference
+    algorithm on the CPU) against the GPU adjoint: start parameters of 100
+    tracks, the field scale and the six alignment parameters of one plane."""
+    tel = kf.make_telescope(100, seed=99, **TEL)
+    cfg = kf.default_config(overstep_limit=0.1)
+    ab = kf.AdjointBatch(tel, cfg)
+    r = ab.run(grad=True)
+    ok = r["status"] == 0
+
+    def ochi2(start=None, field_scale=1.0, center=None, rotation=None):
+        t = tel
+        if start is not None:
+            import copy
+            t = copy.copy(tel)
+            t.start = start
+        o = orc.fit(t, cfg, threads=0, smoothed=True, field_scale=field_scale, center=center,
+                    rotation=rotation, variant="precise")
+        return chi2_from_smoothed(kf, tel, o["smoothed"], o["status"])
+
+    base = ochi2()
+    assert np.allclose(base[ok], r["chi2"][ok], rtol=1e-9)
+    for e in range(5):
+        h = 1e-4 * np.maximum(np.abs(tel.start[e]), START_SCALE[e])
+
+        def f(d):
+            sp = tel.start.copy()
+            sp[e] += d
+            return ochi2(start=sp)
+
+        fd = _fd4(f, h)
+        rel = _rel(r["grad_start"][e][ok], fd[ok], np.median(np.abs(fd[ok])))
+        assert np.median(rel) < 3e-7 and np.quantile(rel, 0.98) < 3e-6, (e, np.sort(rel)[-4:])
+    fd = _fd4(lambda d: ochi2(field_scale=1 + d)[ok].sum(), 1e-5)
+    assert abs(r["grad_field_scale"][0] - fd) <= 1e-6 * abs(fd)
+    k = 7
+    for a in range(6):
+        def f(d):
+            al = np.zeros((tel.n_surfaces, 6))
+            al[k, a] = d
+            c1, r1 = kf.align_geometry(tel.center, tel.rotation, al)
+            return ochi2(center=c1, rotation=r1)[ok].sum()
+        fd = _fd4(f, 1e-4 * ALIGN_SCALE[a])
+        assert abs(r["grad_align"][k, a] - fd) <= 1e-6 * max(abs(fd), 1e-3 * np.max(np.abs(r["grad_align"][:, a]))), (a, r["grad_align"][k, a], fd)
+
+
+def test_gradcheck_through_autograd(kf):
+    torch = pytest.importorskip("torch")
+    from gpukalmanfitter_gb300.autograd import Chi2
+    tel = kf.make_telescope(16, seed=5, **TEL)
+    ab = kf.AdjointBatch(tel, kf.default_config(overstep_limit=0.1))
+    start = torch.tensor(tel.start, dtype=torch.float64, requires_grad=True)
+    align = torch.zeros((tel.n_surfaces, 6), dtype=torch.float64, requires_grad=True)
+    fs = torch.tensor(1.0, dtype=torch.float64, requires_grad=True)
+    # FD steps sized for mm / rad / 1/GeV inputs
+    assert torch.autograd.gradcheck(lambda s, a, f: Chi2.apply(s, a, f, ab), (start, align, fs),
+                                    eps=1e-6, atol=1e-3, rtol=1e-4)
+
+
+def test_adjoint_rejects_unsupported(kf):
+    tel = kf.make_telescope(10, seed=1, n_planes=10, field_map=True, field_n=11)
+    with pytest.raises(kf.KfError):
+        kf.AdjointBatch(tel, kf.default_config()).run(grad=True)
