@@ -440,7 +440,7 @@ def fit_device(tel: Telescope, cfg: KfConfig | None = None, **kw) -> dict:
 class KfAdjointOutputs(C.Structure):
     _fields_ = [("chi2", C.c_void_p), ("status", C.c_void_p), ("grad_start", C.c_void_p),
                 ("grad_align", C.c_void_p), ("grad_field_scale", C.c_void_p),
-                ("chi2_total", C.c_void_p)]
+                ("chi2_total", C.c_void_p), ("grad_field_scale_track", C.c_void_p)]
 
 
 def _rot(a: np.ndarray) -> np.ndarray:
@@ -489,10 +489,12 @@ class AdjointBatch:
                     "grad_start": torch.zeros((6, n), dtype=torch.float64, device=device),
                     "grad_align": torch.zeros((S, 6), dtype=torch.float64, device=device),
                     "grad_field_scale": torch.zeros(1, dtype=torch.float64, device=device),
-                    "chi2_total": torch.zeros(1, dtype=torch.float64, device=device)}
+                    "chi2_total": torch.zeros(1, dtype=torch.float64, device=device),
+                    "grad_field_scale_track": torch.zeros(n, dtype=torch.float64, device=device)}
         self.aout = KfAdjointOutputs(*[self.out[k].data_ptr() for k in
                                        ("chi2", "status", "grad_start", "grad_align",
-                                        "grad_field_scale", "chi2_total")])
+                                        "grad_field_scale", "chi2_total",
+                                        "grad_field_scale_track")])
         lib = load()
         self.ws_bytes = int(lib.kf_adjoint_workspace_size(C.byref(self.cfg), n, S))
         if n > 0 and self.ws_bytes < n * S * 37 * 8:

@@ -236,24 +236,28 @@ __device__ __forceinline__ bool hitPending(const ALane &L) {
          ((L.mask >> L.current) & 1ull);
 }
 
-// Run the lane program until it is done, or until it is parked before the hit
-// event of measurement state stopAt (stopAt < 0: never).  With ck, save the
-// lane before the hit events of states 5, 10, ...
-__device__ void runLane(ALane &L, const Params &P, const PlaneD *sp, const AdjParams &A,
+// Run the lane program of every lane of the warp (all 32 lanes call it) until
+// each is done or parked before the hit event of measurement state stopAt
+// (stopAt < 0: never).  As in the fit kernel, lanes step independently and
+// run their surface events together once every lane waits.  With ck, a lane
+// saves itself before the hit events of states 5, 10, ...
+__device__ void runWarp(ALane &L, const Params &P, const PlaneD *sp, const AdjParams &A,
                         int stopAt, bool ck) {
+  bool stopped = false;
   for (;;) {
-    if (!L.parked && L.pc != PC_DONE) advance(L, P, sp);
-    if (L.parked) {
-      if (hitPending(L) && L.measStates > 0 && L.measStates % kEvery == 0) {
-        if (L.measStates == stopAt) return;
-        if (ck) {
+    if (!L.parked && !stopped && L.pc != PC_DONE) advance(L, P, sp);
+    if (L.parked && !stopped && hitPending(L) && L.measStates == stopAt) stopped = true;
+    const bool waiting = L.parked || stopped || L.pc == PC_DONE;
+    if (__all_sync(0xffffffffu, waiting)) {
+      if (L.parked && !stopped) {
+        if (ck && hitPending(L) && L.measStates > 0 && L.measStates % kEvery == 0) {
           Saver s{A.snap + (int64_t)(L.measStates / kEvery - 1) * kSnapWords * P.n + L.idx, P.n, 0};
           visitLane(L, s);
         }
+        runEvent(L, P, sp);
       }
-      runEvent(L, P, sp);
+      if (__all_sync(0xffffffffu, stopped || L.pc == PC_DONE)) return;
     }
-    if (L.pc == PC_DONE) return;
   }
 }
 
@@ -462,19 +466,36 @@ __device__ void reverseHit(const double *w, Adj &R, const Params &P, const Plane
   addAlign(A, n, i, k, f, fb);
 }
 
-__device__ bool reverseTape(const double *tape, int top, Adj &R, const Params &P,
+// Sweep the tapes of all lanes backwards together: step and navigation
+// records whenever a lane has one on top, surface events once every lane with
+// work has one on top.  Returns false for a malformed tape.
+__device__ bool reverseWarp(const double *tape, int top, Adj &R, const Params &P,
                             const PlaneD *sp, const AdjParams &A, int64_t i, double q) {
-  while (top > 0) {
-    const int h = (int)tape[top - 1];
-    const int type = h >> 16, len = h & 0xffff;
-    if (len < 2 || len > top || type < REC_STEP || type > REC_HIT) return false;
-    const double *w = tape + (top - len);
-    if (type == REC_STEP) reverseStep(w, len, R, P, q);
-    else if (type == REC_ACT) reverseAct(w, R, sp, A, P.n, i);
-    else reverseHit(w, R, P, sp, A, i, q);
-    top -= len;
+  bool bad = false;
+  for (;;) {
+    int type = 0, len = 0;
+    if (top > 0 && !bad) {
+      const int h = (int)tape[top - 1];
+      type = h >> 16;
+      len = h & 0xffff;
+      if (len < 2 || len > top || type < REC_STEP || type > REC_HIT) {
+        bad = true;
+        type = 0;
+      }
+    }
+    if (__any_sync(0xffffffffu, type == REC_STEP || type == REC_ACT)) {
+      if (type == REC_STEP) reverseStep(tape + (top - len), len, R, P, q);
+      else if (type == REC_ACT) reverseAct(tape + (top - len), R, sp, A, P.n, i);
+      if (type == REC_STEP || type == REC_ACT) top -= len;
+    } else {
+      if (!__any_sync(0xffffffffu, type == REC_HIT)) break;
+      if (type == REC_HIT) {
+        reverseHit(tape + (top - len), R, P, sp, A, i, q);
+        top -= len;
+      }
+    }
   }
-  return true;
+  return !bad;
 }
 
 // smoothed chi2 of one track from its stored states; with grad, the adjoints
@@ -567,45 +588,58 @@ __global__ void __launch_bounds__(kLaneSlots) adjointKernel(const __grid_constan
   __shared__ PlaneD sp[KF_MAX_PLANES];
   for (int k = threadIdx.x; k < P.nSurf; k += blockDim.x) sp[k] = P.planes[k];
   __syncthreads();
+  // every lane stays to the end: the lane program and the reverse sweep run
+  // warp-synchronously (idle lanes carry no work)
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= P.n) return;
+  const bool valid = i < P.n;
   ALane L;
-  L.hook.tape = A.tape + i * kTapeWords;
-  L.hook.info = A.info + i;
+  L.hook.tape = A.tape + (valid ? i : 0) * kTapeWords;
+  L.hook.info = A.info + (valid ? i : 0);
   L.hook.n = P.n;
   L.hook.top = L.hook.head = L.hook.state = L.hook.plane = 0;
   L.hook.rec = false;
   L.hook.full = false;
-  zeroTrack(P, A, i);
+  if (valid) zeroTrack(P, A, i);
   // ---- A: forward fit with checkpoints
-  initLane(L, P, sp, i, i);
-  if (L.pc != PC_DONE) runLane(L, P, sp, A, -1, A.grad != 0);
+  initLane(L, P, sp, valid ? i : -1, valid ? i : 0);
+  runWarp(L, P, sp, A, -1, A.grad != 0);
   const int ns = L.measStates;
-  A.status[i] = L.status;
-  if (L.status != KF_TRACK_OK || ns == 0) return;
+  const bool ok = valid && L.status == KF_TRACK_OK && ns > 0;
+  if (valid) A.status[i] = L.status;
   // ---- B: smoothed chi2 (and the smoother's adjoints)
-  A.chi2[i] = smoothChi2(P, A, i, ns, A.grad != 0);
+  if (ok) A.chi2[i] = smoothChi2(P, A, i, ns, A.grad != 0);
   if (!A.grad) return;
-  // ---- C: segments, last first
+  // ---- C: segments, last first, all lanes together
   Adj R;
   adjZero(R);
   const double q = L.q;
-  const int nseg = (ns - 1) / kEvery + 1;
-  for (int c = nseg - 1; c >= 0; --c) {
+  const int nseg = ok ? (ns - 1) / kEvery + 1 : 0;
+  const int maxSeg = __reduce_max_sync(0xffffffffu, nseg);
+  bool failed = false;
+  for (int c = maxSeg - 1; c >= 0; --c) {
+    const bool act = ok && !failed && c < nseg;
     L.hook.top = 0;
-    L.hook.rec = true;
-    if (c == 0) {
+    L.hook.rec = act;
+    if (!act) {
+      L.pc = PC_DONE;
+      L.parked = false;
+    } else if (c == 0) {
       initLane(L, P, sp, i, i);
     } else {
       Loader ld{A.snap + (int64_t)(c - 1) * kSnapWords * P.n + i, P.n, 0};
       visitLane(L, ld);
     }
-    runLane(L, P, sp, A, (c + 1) * kEvery, false);
-    if (L.hook.full || !reverseTape(L.hook.tape, L.hook.top, R, P, sp, A, i, q)) {
-      A.status[i] = KF_TRACK_ADJOINT_FAILED;
-      zeroTrack(P, A, i);
-      return;
-    }
+    runWarp(L, P, sp, A, (c + 1) * kEvery, false);
+    if (act && L.hook.full) failed = true;
+    const bool sweep = act && !failed;
+    if (!reverseWarp(L.hook.tape, sweep ? L.hook.top : 0, R, P, sp, A, i, q) && sweep)
+      failed = true;
+  }
+  if (!ok) return;
+  if (failed) {
+    A.status[i] = KF_TRACK_ADJOINT_FAILED;
+    zeroTrack(P, A, i);
+    return;
   }
   // ---- start parameters: the leg constants belong to the start momentum
   double sp0[6];
@@ -725,7 +759,9 @@ int32_t kf_adjoint_batch(const kf_inputs_t *in, kf_adjoint_outputs_t *out, const
   A.snap = reinterpret_cast<double *>(base + L.snap);
   A.tape = reinterpret_cast<double *>(base + L.tape);
   A.alignPart = reinterpret_cast<double *>(base + L.alignPart);
-  A.trackFs = reinterpret_cast<double *>(base + L.trackFs);
+  A.trackFs = (compute_gradient && out->grad_field_scale_track)
+                  ? out->grad_field_scale_track
+                  : reinterpret_cast<double *>(base + L.trackFs);
   A.chi2 = out->chi2;
   A.status = out->status;
   A.gradStart = compute_gradient ? out->grad_start : nullptr;

@@ -285,6 +285,7 @@ typedef struct kf_adjoint_outputs {
   double *grad_align;       /* [n_surfaces][6] d chi2_total / d alignment, or NULL */
   double *grad_field_scale; /* [1] d chi2_total / d field scale, or NULL */
   double *chi2_total;       /* [1] total chi2, or NULL */
+  double *grad_field_scale_track; /* [n] d chi2_track / d field scale, or NULL */
 } kf_adjoint_outputs_t;
 
 size_t kf_adjoint_workspace_size(const kf_config_t *cfg, int64_t n_tracks, int32_t n_surfaces);

@@ -106,8 +106,12 @@ def test_alignment_gradient_matches_finite_differences(ab):
 
 def test_field_scale_gradient_matches_finite_differences(ab):
     r = ab.run(grad=True)
-    fd = _fd4(lambda d: ab.run(grad=False, field_scale=1 + d)["chi2_total"][0], 1e-5)
-    assert abs(r["grad_field_scale"][0] - fd) <= 1e-6 * abs(fd)
+    ok = r["status"] == 0
+    g = r["grad_field_scale_track"]
+    fd = _fd4(lambda d: ab.run(grad=False, field_scale=1 + d)["chi2"], 1e-4)
+    rel = _rel(g[ok], fd[ok], np.median(np.abs(fd[ok])))
+    assert np.median(rel) < 3e-7 and np.quantile(rel, 0.99) < 3e-6, np.sort(rel)[-4:]
+    assert abs(r["grad_field_scale"][0] - g[ok].sum()) <= 1e-9 * np.abs(g[ok]).sum()
 
 
 def test_reference_forward_gradient(kf, orc):
@@ -143,8 +147,9 @@ def test_reference_forward_gradient(kf, orc):
         fd = _fd4(f, h)
         rel = _rel(r["grad_start"][e][ok], fd[ok], np.median(np.abs(fd[ok])))
         assert np.median(rel) < 3e-7 and np.quantile(rel, 0.98) < 3e-6, (e, np.sort(rel)[-4:])
-    fd = _fd4(lambda d: ochi2(field_scale=1 + d)[ok].sum(), 1e-5)
-    assert abs(r["grad_field_scale"][0] - fd) <= 1e-6 * abs(fd)
+    fd = _fd4(lambda d: ochi2(field_scale=1 + d), 1e-4)
+    rel = _rel(r["grad_field_scale_track"][ok], fd[ok], np.median(np.abs(fd[ok])))
+    assert np.median(rel) < 3e-7 and np.quantile(rel, 0.98) < 3e-6, np.sort(rel)[-4:]
     k = 7
     for a in range(6):
         def f(d):
