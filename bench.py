@@ -10,8 +10,10 @@ one CUDA-graph launch (work-queue sort + persistent fit kernel, shape picked
 by the autotuner beforehand), in the plain form one grid kernel launch.  The
 line carries both forms on the same batch ("forms"), and a suite of two more
 one-GPU comparisons: 4M uneven tracks with holes and outliers on 30 planes,
-and 1M tracks on 30 planes in the FP32 field map (plain FP64 against batched
-FP64 and batched mixed precision).
+1M tracks on 30 planes in the FP32 field map (plain FP64 against batched FP64
+and batched mixed precision), and the chi2 adjoint (gradients with respect to
+plane alignment, start parameters and field scale) on 256k tracks of a
+misaligned 20-plane telescope against one forward fit of the same batch.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
                   [--form batched|plain] [--workload W] [--precision fp64|mixed]
@@ -39,7 +41,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-METRIC = "fitted tracks/s (Kalman fit: RK4 propagation + gain-matrix filter + RTS smoother + perigee transport)"
+METRIC = "fitted tracks/s on 1 GB300, plain vs batched form at equal accuracy; grads/s"
 UNIT = "tracks/s"
 OVERSTEP = 0.1  # mm; the reference's fixed 0.01 mm skips planes on this workload
 CPU_SAMPLE = 100_000
@@ -57,6 +59,10 @@ WORKLOADS = {
                      outlier_prob=0.02), dict(outlier_chi2_cut=25.0)),
 }
 PRECISIONS = {"fp64": 0, "mixed": 1}
+# chi2 adjoint workload: truth planes misaligned, the fit uses the nominal geometry
+ALIGN20 = ("telescope of 20 planes x=50..1000 mm, uniform 2 T, truth planes misaligned by "
+           "N(0, 100 um) shifts and N(0, 1 mrad) rotations (nominal geometry in the fit)",
+           dict(n_planes=20, x_first=50., x_step=50., mis_shift=0.1, mis_rot=1e-3))
 
 
 def workload_config(name: str, n_tracks: int, precision: str) -> dict:
@@ -210,10 +216,16 @@ def timed_steps(step, stream, steps: int, warmup: int, barrier) -> tuple:
     return t_start.elapsed_time(t_end), [a.elapsed_time(b) for a, b in evs]
 
 
-def batched_step(batch, stream) -> tuple:
-    """Autotune the persistent kernel shape on this batch, capture the sort and
-    the fit into a CUDA graph; one step = one graph launch (4 kernels)."""
-    tuned, tune_ms = batch.autotune(stream)
+def batched_step(batch, stream, ctas_per_sm: int = 0) -> tuple:
+    """Autotune the persistent kernel shape on this batch (or take the given
+    CTAs per SM), capture the sort and the fit into a CUDA graph; one step =
+    one graph launch (4 kernels)."""
+    if ctas_per_sm:
+        batch.cfg.block_size, batch.cfg.min_blocks_per_sm = 128, ctas_per_sm
+        batch.cfg.kernel = 2
+        tuned, tune_ms = batch.cfg, 0.0
+    else:
+        tuned, tune_ms = batch.autotune(stream)
     batch.make_plan(stream)
     shape = {"threads_per_cta": tuned.block_size, "ctas_per_sm": tuned.min_blocks_per_sm,
              "tracks_per_warp": 32, "autotune_best_ms_on_sample": round(tune_ms, 3)}
@@ -248,6 +260,54 @@ def suite_entry(kf, name: str, n: int, seed: int, stream, barrier, steps: int, w
     return out
 
 
+def adjoint_entry(kf, n: int, seed: int, stream, barrier, steps: int, warmup: int) -> dict:
+    """d(total smoothed chi2)/d(alignment 6 x 20, start parameters 6 per track,
+    field scale) with kf_adjoint_batch, against one forward fit of the same
+    batch (plain FP64 grid kernel and batched form)."""
+    import torch
+    tel = kf.make_telescope(n, seed=seed, **ALIGN20[1])
+    cfg = kf.default_config(overstep_limit=OVERSTEP)
+    with torch.cuda.stream(stream):
+        fit = kf.DeviceBatch(tel, cfg)
+    fit_ms, _ = timed_steps(lambda: fit.fit(stream), stream, steps, warmup, barrier)
+    fit_ms /= steps
+    step, _, shape = batched_step(fit, stream)
+    bat_ms, _ = timed_steps(step, stream, steps, warmup, barrier)
+    bat_ms /= steps
+    fit.destroy_plan()
+    del fit
+    torch.cuda.empty_cache()
+    with torch.cuda.stream(stream):
+        ab = kf.AdjointBatch(tel, cfg)
+    lib = kf.load()
+    geo, keep = tel.geometry()
+    field = tel.field(scale=1.0)
+
+    def call(grad):
+        rc = lib.kf_adjoint_batch(C.byref(ab.ins), C.byref(ab.aout), C.byref(ab.cfg),
+                                  C.byref(geo), C.byref(field), C.c_int32(grad),
+                                  C.c_void_p(ab.ws.data_ptr()), C.c_size_t(ab.ws_bytes),
+                                  C.c_void_p(stream.cuda_stream))
+        if rc != 0:
+            raise RuntimeError(lib.kf_last_error_string().decode())
+
+    adj_ms, _ = timed_steps(lambda: call(1), stream, steps, warmup, barrier)
+    adj_ms /= steps
+    fwd_ms, _ = timed_steps(lambda: call(0), stream, steps, warmup, barrier)
+    fwd_ms /= steps
+    st = ab.out["status"].cpu().numpy()
+    del ab
+    torch.cuda.empty_cache()
+    return {"workload": f"align20: {ALIGN20[0]}", "tracks": n,
+            "gradients": "d chi2_total / d (6 x 20 alignment, 6 start parameters per track, field scale)",
+            "tracks_differentiated_per_s": n / (adj_ms * 1e-3),
+            "adjoint_ms": adj_ms, "adjoint_forward_only_ms": fwd_ms,
+            "fit_plain_fp64_ms": fit_ms, "fit_batched_fp64_ms": bat_ms,
+            "adjoint_over_plain_fit": adj_ms / fit_ms, "adjoint_over_batched_fit": adj_ms / bat_ms,
+            "differentiated_fraction": float((st == 0).mean()),
+            "checkpoint_every_states": 5}
+
+
 def run_gpu(args) -> None:
     import torch
     import gpukalmanfitter_gb300 as kf
@@ -275,7 +335,7 @@ def run_gpu(args) -> None:
     torch.cuda.synchronize()
     shape = None
     if args.form == "batched":
-        step, per_step, shape = batched_step(batch, stream)
+        step, per_step, shape = batched_step(batch, stream, args.ctas_per_sm)
     else:
         step, per_step = (lambda: batch.fit(stream)), 1
 
@@ -307,7 +367,7 @@ def run_gpu(args) -> None:
     rc = lib.kf_diag_fp64_fma_rate(C.c_int32(20000), C.byref(peak), C.c_void_p(stream.cuda_stream))
     peak_tflops = peak.value / 1e3 if rc == 0 else None
     achieved = flop / avg_launch_s / 1e12
-    traffic = traffic_estimate(args, n)
+    traffic = traffic_estimate(args, n, shape)
     mb = F.batch_bytes(n, tel.n_surfaces)
     hbm_peak, hbm_src = hbm_peak_gbs()
 
@@ -323,14 +383,18 @@ def run_gpu(args) -> None:
     torch.cuda.empty_cache()
 
     suite = None
-    if not args.no_suite and world == 1:
-        # uneven tracks (4x the headline batch) and the field map (1x)
-        suite = {
-            "batching": suite_entry(kf, "holes30", 4 * n, 1234567892, stream, barrier, 3, 3,
-                                    [("batched_fp64", "fp64"), ("batched_mixed", "mixed")]),
-            "precision_map": suite_entry(kf, "map30", n, 1234567893, stream, barrier, 3, 3,
-                                         [("batched_mixed", "mixed"), ("batched_fp64", "fp64")]),
+    wanted = [] if args.no_suite else [x for x in args.suite.split(",") if x and x != "none"]
+    if wanted and world == 1:
+        # uneven tracks (4x the headline batch), the field map (1x), the adjoint (1/4)
+        makers = {
+            "batching": lambda: suite_entry(kf, "holes30", 4 * n, 1234567892, stream, barrier, 3, 3,
+                                            [("batched_fp64", "fp64"), ("batched_mixed", "mixed")]),
+            "precision_map": lambda: suite_entry(kf, "map30", n, 1234567893, stream, barrier, 3, 3,
+                                                 [("batched_mixed", "mixed"), ("batched_fp64", "fp64")]),
+            "differentiation": lambda: adjoint_entry(kf, max(1, n // 4), 1234567894, stream,
+                                                     barrier, 3, 3),
         }
+        suite = {k: makers[k]() for k in makers if k in wanted}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -378,14 +442,17 @@ def run_gpu(args) -> None:
         dist.destroy_process_group()
 
 
-def traffic_estimate(args, n: int):
+def traffic_estimate(args, n: int, shape):
     """DRAM bytes per launch from a committed ncu capture of the same kernel
-    and workload (scaled by tracks), or None."""
+    instantiation and workload (scaled by tracks), or None."""
     tfile = ROOT / "profiles" / "traffic.json"
     if not tfile.exists():
         return None
+    key = f"{args.workload}/{args.precision}/{args.form}"
+    if shape:
+        key += f"/ctas{shape['ctas_per_sm']}"
     try:
-        rec = json.loads(tfile.read_text()).get(f"{args.workload}/{args.precision}/{args.form}")
+        rec = json.loads(tfile.read_text()).get(key)
         return rec["dram_bytes_per_track"] * n if rec else None
     except (ValueError, KeyError, TypeError):
         return None
@@ -475,7 +542,11 @@ def main() -> None:
                     help="batched: sorted queue + persistent kernel in a CUDA graph; "
                          "plain: one thread per track, grid over the batch")
     ap.add_argument("--no-suite", action="store_true",
-                    help="skip the uneven-track and field-map comparisons")
+                    help="skip the uneven-track, field-map and adjoint comparisons")
+    ap.add_argument("--ctas-per-sm", type=int, default=0, choices=[0, 2, 3, 4, 5],
+                    help="batched form: persistent kernel shape (0 = autotune)")
+    ap.add_argument("--suite", default="batching,precision_map,differentiation",
+                    help="comma list of suite entries to run (or 'none')")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -107,13 +107,14 @@ struct TapeHook {
     if (!ok) full = true; // a failed step has no derivative: the track is dropped
     put(hdr(REC_STEP, top + 1 - head));
   }
-  template <class LT> __device__ __forceinline__ void actorSet(const LT &L, int k) {
+  // A navigation constraint is always set from the state the next RK step
+  // starts from (a hit happens only on a surface, where the constraint is
+  // released instead), so the record keeps the plane only; the reverse sweep
+  // takes the state from that step's record.
+  template <class LT> __device__ __forceinline__ void actorSet(const LT &, int k) {
     if (!rec) return;
-    head = top;
-    for (int i = 0; i < 3; ++i) put(L.pos[i]);
-    for (int i = 0; i < 3; ++i) put(L.dir[i]);
     put((double)k);
-    put(hdr(REC_ACT, 8));
+    put(hdr(REC_ACT, 2));
   }
   template <class LT> __device__ __forceinline__ void hitBegin(const LT &L, int k) {
     state = L.measStates;
@@ -369,16 +370,17 @@ __device__ void reverseStep(const double *w, int len, Adj &R, const Params &P, d
   R.J = Jb0;
 }
 
-// reverse of a navigation step-constraint update (distance to plane k)
-__device__ void reverseAct(const double *w, Adj &R, const PlaneD *sp, const AdjParams &A,
-                           int64_t n, int64_t i) {
+// reverse of a navigation step-constraint update (distance to plane k from
+// the state pos, dir that the following RK step starts from)
+__device__ void reverseAct(const double *w, const double pos[3], const double dir[3], Adj &R,
+                           const PlaneD *sp, const AdjParams &A, int64_t n, int64_t i) {
   if (R.ssAct == 0.) return;
-  const int k = (int)w[6];
+  const int k = (int)w[0];
   kfa::Frame f;
   toFrame(sp[k], f);
   kfa::FrameBar fb;
   kfa::frameBarZero(fb);
-  kfa::pathVjp(w, w + 3, f.c, f.T, R.ssAct, R.pos, R.dir, fb.c, fb.T);
+  kfa::pathVjp(pos, dir, f.c, f.T, R.ssAct, R.pos, R.dir, fb.c, fb.T);
   R.ssAct = 0.;
   addAlign(A, n, i, k, f, fb);
 }
@@ -414,7 +416,10 @@ __device__ void reverseHit(const double *w, Adj &R, const Params &P, const Plane
   toFrame(sp[k], f);
   kfa::BoundOut o, ob;
   kfa::BoundTmp bt;
-  kfa::boundFwd(in, f, o, bt);
+  kfa::boundFwd(in, f, o, bt, false);
+  // predicted and filtered parameters as the forward stored them
+  auto WS = [&](int e) { return P.ws[((int64_t)s * kStateStride + e) * n + i]; };
+  for (int e = 0; e < 6; ++e) o.pred[e] = WS(e);
   // smoother adjoints of this state
   const double *sb = A.stateBar + i;
   auto SB = [&](int e) { return sb[((int64_t)s * kStateStride + e) * n]; };
@@ -431,8 +436,8 @@ __device__ void reverseHit(const double *w, Adj &R, const Params &P, const Plane
     double filt[6], cf[21], chi2;
     kfa::FilterTmp fw;
     kfa::filterFwd(o.pred, o.Cp, mv, filt, cf, &chi2, fw);
-    double pos1[3], dir1[3], p1, t1;
-    kfa::updateFwd(f, filt, pos1, dir1, &p1, &t1);
+    double pos1[3], dir1[3], p1, t1, trig[4];
+    kfa::updateFwd(f, filt, pos1, dir1, &p1, &t1, trig);
     kfa::Leg g;
     kfa::legFwd(p1, q, P.mass, g);
     double pb = R.p;
@@ -440,7 +445,8 @@ __device__ void reverseHit(const double *w, Adj &R, const Params &P, const Plane
     R.qop = R.dtds = R.d37 = 0.;
     double filtb[6];
     for (int e = 0; e < 6; ++e) filtb[e] = SB(6 + e);
-    kfa::updateVjp(f, filt, dir1, R.pos, R.dir, pb, R.t, filtb, fb);
+    kfa::updateVjp(f, filt, dir1, R.pos, R.dir, pb, R.t, filtb, fb, trig[0], trig[1], trig[2],
+                   trig[3]);
     kfa::filterVjp(o.Cp, fw, filtb, R.C, ob.pred, ob.Cp);
     for (int e = 0; e < 3; ++e) R.pos[e] = R.dir[e] = 0.;
     R.p = R.t = 0.;
@@ -472,6 +478,7 @@ __device__ void reverseHit(const double *w, Adj &R, const Params &P, const Plane
 __device__ bool reverseWarp(const double *tape, int top, Adj &R, const Params &P,
                             const PlaneD *sp, const AdjParams &A, int64_t i, double q) {
   bool bad = false;
+  double cpos[3] = {0., 0., 0.}, cdir[3] = {0., 0., 0.}; // pre-state of the step after
   for (;;) {
     int type = 0, len = 0;
     if (top > 0 && !bad) {
@@ -484,8 +491,16 @@ __device__ bool reverseWarp(const double *tape, int top, Adj &R, const Params &P
       }
     }
     if (__any_sync(0xffffffffu, type == REC_STEP || type == REC_ACT)) {
-      if (type == REC_STEP) reverseStep(tape + (top - len), len, R, P, q);
-      else if (type == REC_ACT) reverseAct(tape + (top - len), R, sp, A, P.n, i);
+      if (type == REC_STEP) {
+        const double *w = tape + (top - len);
+        reverseStep(w, len, R, P, q);
+        for (int e = 0; e < 3; ++e) {
+          cpos[e] = w[e];
+          cdir[e] = w[3 + e];
+        }
+      } else if (type == REC_ACT) {
+        reverseAct(tape + (top - len), cpos, cdir, R, sp, A, P.n, i);
+      }
       if (type == REC_STEP || type == REC_ACT) top -= len;
     } else {
       if (!__any_sync(0xffffffffu, type == REC_HIT)) break;
@@ -583,8 +598,11 @@ __device__ void zeroTrack(const Params &P, const AdjParams &A, int64_t i) {
     for (int e = 0; e < 6; ++e) A.gradStart[(int64_t)e * P.stride + i] = 0.;
 }
 
-__global__ void __launch_bounds__(kLaneSlots) adjointKernel(const __grid_constant__ Params P,
-                                                            const __grid_constant__ AdjParams A) {
+#ifndef KF_ADJ_MIN_BLOCKS
+#define KF_ADJ_MIN_BLOCKS 2
+#endif
+__global__ void __launch_bounds__(kLaneSlots, KF_ADJ_MIN_BLOCKS)
+    adjointKernel(const __grid_constant__ Params P, const __grid_constant__ AdjParams A) {
   __shared__ PlaneD sp[KF_MAX_PLANES];
   for (int k = threadIdx.x; k < P.nSurf; k += blockDim.x) sp[k] = P.planes[k];
   __syncthreads();

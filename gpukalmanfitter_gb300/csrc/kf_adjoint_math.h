@@ -576,7 +576,11 @@ struct BoundTmp {
   DirCoef k;
 };
 
-KF_HD void boundFwd(const BoundIn &in, const Frame &f, BoundOut &o, BoundTmp &w) {
+// full = false: the reverse sweep's recomputation; the predicted parameters
+// come from the stored state and only covariance rows 0-1 (all the gain and
+// its adjoint read) are formed
+KF_HD void boundFwd(const BoundIn &in, const Frame &f, BoundOut &o, BoundTmp &w,
+                    bool full = true) {
   for (int r = 0; r < 3; ++r) {
     w.Pt0[r][0] = in.G.g03[r][0];
     w.Pt0[r][1] = in.G.g03[r][1];
@@ -626,7 +630,7 @@ KF_HD void boundFwd(const BoundIn &in, const Frame &f, BoundOut &o, BoundTmp &w)
       for (int k = 0; k < 6; ++k) s += J[i][k] * in.C[si6(k, j)];
       w.M[i][j] = s;
     }
-  for (int i = 0; i < 6; ++i)
+  for (int i = 0; i < (full ? 6 : 2); ++i)
     for (int j = i; j < 6; ++j) {
       double s = 0.;
       for (int k = 0; k < 6; ++k) s += w.M[i][k] * J[j][k];
@@ -647,6 +651,7 @@ KF_HD void boundFwd(const BoundIn &in, const Frame &f, BoundOut &o, BoundTmp &w)
     o.G.g46[r][0] = w.k.g46[r][0];
     o.G.g46[r][1] = w.k.g46[r][1];
   }
+  if (!full) return;
   double dd[3];
   for (int i = 0; i < 3; ++i) dd[i] = in.pos[i] - f.c[i];
   o.pred[0] = dot(f.U, dd);
@@ -727,22 +732,27 @@ KF_HD void boundVjp(const BoundIn &in, const Frame &f, const BoundOut &o, const 
       Jb[i][j] = 0.;
     }
   const double(&J)[6][6] = w.Jf;
-  // Jb = (W + W^T) J C ; J C = M
-  for (int a = 0; a < 6; ++a)
-    for (int b = 0; b < 6; ++b) {
+  // Jb = (W + W^T) J C = (W + W^T) M, on the free entries (rows 0-3,5, cols 0-4)
+  for (int a = 0; a < 6; ++a) {
+    if (a == 4) continue;
+    for (int b = 0; b < 5; ++b) {
       double s = 0.;
       for (int i = 0; i < 6; ++i) s += (W[a][i] + W[i][a]) * w.M[i][b];
       Jb[a][b] += s;
     }
-  // C-bar (full) = J^T W J, folded onto the stored upper triangle
+  }
+  // C-bar (full) = J^T (W J), folded onto the stored upper triangle
+  double WJ[6][6];
+  for (int i = 0; i < 6; ++i)
+    for (int l = 0; l < 6; ++l) {
+      double t = 0.;
+      for (int j = 0; j < 6; ++j) t += W[i][j] * J[j][l];
+      WJ[i][l] = t;
+    }
   for (int k = 0; k < 6; ++k)
     for (int l = 0; l < 6; ++l) {
       double s = 0.;
-      for (int i = 0; i < 6; ++i) {
-        double t = 0.;
-        for (int j = 0; j < 6; ++j) t += W[i][j] * J[j][l];
-        s += J[i][k] * t;
-      }
+      for (int i = 0; i < 6; ++i) s += J[i][k] * WJ[i][l];
       ib.C[si6(k, l)] += s;
     }
   for (int c = 0; c < 5; ++c) {
@@ -899,17 +909,25 @@ KF_HD void filterVjp(const double C[21], const FilterTmp &w, const double filtb[
 //   p = |1/x4|, t = x5;  qop = q/p, dtds = hypot(1, m/p), d37 = m^2 q/(p dtds)
 // ---------------------------------------------------------------------------
 KF_HD void updateFwd(const Frame &f, const double x[6], double pos[3], double d[3], double *p,
-                     double *t) {
+                     double *t, double trig[4] = nullptr) {
   for (int r = 0; r < 3; ++r) pos[r] = f.U[r] * x[0] + f.V[r] * x[1] + f.c[r];
   const double sp = sin(x[2]), cp = cos(x[2]), st = sin(x[3]), ct = cos(x[3]);
+  if (trig) {
+    trig[0] = sp;
+    trig[1] = cp;
+    trig[2] = st;
+    trig[3] = ct;
+  }
   const double v[3] = {cp * st, sp * st, ct};
   const double n = sqrt(dot(v, v));
   for (int i = 0; i < 3; ++i) d[i] = v[i] / n;
   *p = fabs(1. / x[4]);
   *t = x[5];
 }
+// sp, cp, st, ct: sin/cos of x[2] and x[3] (as evaluated by updateFwd)
 KF_HD void updateVjp(const Frame &f, const double x[6], const double d[3], const double posb[3],
-                     const double db[3], double pb, double tb, double xb[6], FrameBar &fb) {
+                     const double db[3], double pb, double tb, double xb[6], FrameBar &fb,
+                     double sp, double cp, double st, double ct) {
   for (int r = 0; r < 3; ++r) {
     xb[0] += posb[r] * f.U[r];
     xb[1] += posb[r] * f.V[r];
@@ -917,7 +935,6 @@ KF_HD void updateVjp(const Frame &f, const double x[6], const double d[3], const
     fb.V[r] += posb[r] * x[1];
     fb.c[r] += posb[r];
   }
-  const double sp = sin(x[2]), cp = cos(x[2]), st = sin(x[3]), ct = cos(x[3]);
   const double v[3] = {cp * st, sp * st, ct};
   const double n = sqrt(dot(v, v));
   const double pr = dot(d, db);

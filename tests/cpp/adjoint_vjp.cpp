@@ -482,12 +482,13 @@ static double testUpdate() {
     Vec yb = randv(8);
     Frame fr;
     unpackFrame(&x[6], fr);
-    double pos[3], d[3], p, tt;
-    updateFwd(fr, &x[0], pos, d, &p, &tt);
+    double pos[3], d[3], p, tt, trig[4];
+    updateFwd(fr, &x[0], pos, d, &p, &tt, trig);
     Vec xb(6, 0.);
     FrameBar fb;
     frameBarZero(fb);
-    updateVjp(fr, &x[0], d, &yb[0], &yb[3], yb[6], yb[7], &xb[0], fb);
+    updateVjp(fr, &x[0], d, &yb[0], &yb[3], yb[6], yb[7], &xb[0], fb, trig[0], trig[1], trig[2],
+              trig[3]);
     xb.insert(xb.end(), fb.c, fb.c + 3);
     xb.insert(xb.end(), fb.U, fb.U + 3);
     xb.insert(xb.end(), fb.V, fb.V + 3);
