@@ -35,7 +35,7 @@ namespace adj {
 
 constexpr int kEvery = 5;          // measurement states per checkpointed segment
 constexpr int kTapeWords = 3072;   // tape capacity per track and segment (doubles)
-constexpr int kSnapWords = 116;    // doubles per lane checkpoint
+constexpr int kSnapWords = 128;    // doubles per lane checkpoint (visitLane writes 115)
 enum { REC_STEP = 1, REC_ACT = 2, REC_HIT = 3 };
 constexpr int kStepFixed = 33;     // pos 3, dir 3, t, p, transport Jacobian 25
 
@@ -193,6 +193,13 @@ template <class V> __device__ void visitLane(ALane &L, V &v) {
   v(L.next);
   v(L.current);
   v(L.nSeq);
+  v(L.navCache);
+  v(L.navCacheSt);
+  {
+    int64_t x = L.navCacheLim;
+    v(x);
+    L.navCacheLim = x;
+  }
   v(L.mask);
   v(L.nHits);
   v(L.measStates);

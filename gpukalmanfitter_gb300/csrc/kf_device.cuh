@@ -32,6 +32,8 @@
 // its step sequence follows the FP64 fit's.
 #pragma once
 
+#include <type_traits>
+
 #include <cfloat>
 #include <cstdint>
 
@@ -237,6 +239,8 @@ template <typename R, typename H = NoHook> struct Lane {
   double qop, dtds, d37;
   // ---- navigation / actor
   int next, current, nSeq; // current: -1 none, >=0 plane, -2 target line
+  int navCache, navCacheSt; // plane and status of the last status() intersection (-1: none)
+  long long navCacheLim;    // the path limit (aborter constraint) it was judged against
   uint64_t mask;
   int nHits, measStates, firstPlane;
   bool targetReached, navBreak, smoothed, finished, result, tn, parked;
@@ -685,31 +689,38 @@ __device__ __forceinline__ void projectCov(Lane<R, H> &L, Transported<R> &X, con
   const R cosP = x * invS, sinP = y * invS;
   const R j24 = -sinP * invS, j25 = cosP * invS;
   const R j34 = cosP * cosT, j35 = sinP * cosT, j36 = -sinT;
-  double J[6][6];
+  // the projection's arithmetic type: the Jacobian's (FP32 in the mixed form:
+  // covariance transport is Jacobian transport; the covariance itself stays
+  // FP64 between events, and the gain and Joseph update are FP64)
+  using CT = typename std::conditional<sizeof(R) == sizeof(float), float, double>::type;
+  CT J[6][6];
 #pragma unroll
   for (int c = 0; c < 5; ++c) {
     J[0][c] = ax0[0] * X.Pt[0][c] + ax0[1] * X.Pt[1][c] + ax0[2] * X.Pt[2][c];
     J[1][c] = ax1[0] * X.Pt[0][c] + ax1[1] * X.Pt[1][c] + ax1[2] * X.Pt[2][c];
     J[2][c] = j24 * X.Dd[0][c] + j25 * X.Dd[1][c];
     J[3][c] = j34 * X.Dd[0][c] + j35 * X.Dd[1][c] + j36 * X.Dd[2][c];
-    J[4][c] = (c == 4) ? 1. : 0.;
+    J[4][c] = (c == 4) ? CT(1) : CT(0);
     J[5][c] = X.R3[c];
   }
 #pragma unroll
-  for (int r = 0; r < 6; ++r) J[r][5] = (r == 5) ? 1. : 0.;
+  for (int r = 0; r < 6; ++r) J[r][5] = (r == 5) ? CT(1) : CT(0);
+  CT Cin[21];
+#pragma unroll
+  for (int e = 0; e < 21; ++e) Cin[e] = (CT)L.cov(e);
   // M = J C  (rows 0-3 and 5 use k = 0..4 (+5 for row 5), row 4 = C row 4)
-  double M[6][6];
+  CT M[6][6];
 #pragma unroll
   for (int i = 0; i < 6; ++i) {
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
       if (i == 4) {
-        M[i][j] = L.cov(sidx(4, j));
+        M[i][j] = Cin[sidx(4, j)];
       } else {
-        double s = J[i][0] * L.cov(sidx(0, j));
+        CT s = J[i][0] * Cin[sidx(0, j)];
 #pragma unroll
-        for (int k = 1; k < 5; ++k) s += J[i][k] * L.cov(sidx(k, j));
-        if (i == 5) s += L.cov(sidx(5, j));
+        for (int k = 1; k < 5; ++k) s += J[i][k] * Cin[sidx(k, j)];
+        if (i == 5) s += Cin[sidx(5, j)];
         M[i][j] = s;
       }
     }
@@ -719,7 +730,7 @@ __device__ __forceinline__ void projectCov(Lane<R, H> &L, Transported<R> &X, con
   for (int i = 0; i < 6; ++i) {
 #pragma unroll
     for (int j = i; j < 6; ++j) {
-      double s;
+      CT s;
       if (j == 4) {
         s = M[i][4];
       } else {
@@ -728,7 +739,7 @@ __device__ __forceinline__ void projectCov(Lane<R, H> &L, Transported<R> &X, con
         for (int k = 1; k < 5; ++k) s += M[i][k] * J[j][k];
         if (j == 5) s += M[i][5];
       }
-      L.cov(ut(i, j)) = s;
+      L.cov(ut(i, j)) = (double)s;
     }
   }
 #pragma unroll
@@ -1251,11 +1262,20 @@ __device__ __forceinline__ int updateSurfaceStatus(Lane<R, H> &L, const Params &
 template <typename R, typename H>
 __device__ __forceinline__ void navStatus(Lane<R, H> &L, const Params &P, const PlaneD *planes) {
   L.current = -1;
+  L.navCache = -1;
   if (L.next != L.nSeq) {
-    if (updateSurfaceStatus(L, P, planes[L.next], L.next) == kOnSurface) {
+    const int st = updateSurfaceStatus(L, P, planes[L.next], L.next);
+    if (st == kOnSurface) {
       L.current = L.next;
       ++L.next;
       if (L.next != L.nSeq) ssRelease(L, kActor);
+    } else {
+      // target() of the same step asks the same plane from the same state: the
+      // state changes between the two only at a surface (never in this branch);
+      // the outcome also depends on the path limit, checked at reuse
+      L.navCache = L.next;
+      L.navCacheSt = st;
+      L.navCacheLim = __double_as_longlong(L.ss[kAborter]);
     }
   }
 }
@@ -1264,7 +1284,11 @@ template <typename R, typename H>
 __device__ __forceinline__ void navTarget(Lane<R, H> &L, const Params &P, const PlaneD *planes) {
   L.current = -1;
   if (L.next != L.nSeq) {
-    if (updateSurfaceStatus(L, P, planes[L.next], L.next) == kMissed) ++L.next;
+    // the repeated intersection would set the same step constraint again
+    const bool reuse = L.navCache == L.next && L.navCacheLim == __double_as_longlong(L.ss[kAborter]);
+    const int st = reuse ? L.navCacheSt : updateSurfaceStatus(L, P, planes[L.next], L.next);
+    L.navCache = -1;
+    if (st == kMissed) ++L.next;
   } else {
     L.navBreak = true;
   }
@@ -1488,6 +1512,9 @@ __device__ void initLane(Lane<R, H> &L, const Params &P, const PlaneD *planes, i
   L.firstPlane = 0;
   L.next = 0;
   L.current = -1;
+  L.navCache = -1;
+  L.navCacheSt = 0;
+  L.navCacheLim = 0;
   L.targetReached = false;
   L.navBreak = false;
   L.smoothed = false;
