@@ -360,7 +360,8 @@ def run_gpu(args) -> None:
     batch.destroy_plan()
 
     ok_frac = float(np.mean(res["status"] == 0))
-    flop = F.batch_flops(res["n_trials"], res["n_steps"], res["n_meas"], res["status"])
+    flop = F.batch_flops(res["n_trials"], res["n_steps"], res["n_meas"], res["status"],
+                         uniform=tel.field_grid is None)
     dense_flop = F.batch_flops(res["n_trials"], res["n_steps"], res["n_meas"], res["status"], dense=True)
     avg_launch_s = statistics.mean(launch_ms) * 1e-3
     peak = C.c_double(0)

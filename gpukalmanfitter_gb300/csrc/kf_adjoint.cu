@@ -321,7 +321,8 @@ __device__ __forceinline__ void routeStep(Adj &R, int idx, double hb) {
   else if (idx == kActor) R.ssAct += hb; // navDir = +1 on the forward leg
 }
 
-// reverse of one RK step record
+// reverse of one RK step record (the uniform-field step of the fit,
+// kfa::polyAcceptFwd, and the error estimates of its rejected trials)
 __device__ void reverseStep(const double *w, int len, Adj &R, const Params &P, double q) {
   const double *pos = w, *dir = w + 3;
   const double t = w[6], p = w[7];
@@ -333,39 +334,33 @@ __device__ void reverseStep(const double *w, int len, Adj &R, const Params &P, d
   kfa::legFwd(p, q, P.mass, g);
   const double *B = P.field.B;
   const double h = tr[2 * (T - 1)];
-  kfa::Stages s;
-  kfa::stagesFwd(dir, g.qop, h, B, s);
-  kfa::Moved m;
-  kfa::acceptFwd(pos, dir, t, h, g.dtds, s, m);
-  kfa::DMat D, Db;
-  kfa::TransportTmp X;
-  kfa::transportFwd(dir, g.qop, h, g.d37, B, s, D, X);
-  double posb[3] = {0., 0., 0.}, dirb[3] = {0., 0., 0.}, tb = 0., hb = 0.;
-  double kb1[3] = {0., 0., 0.}, kb2[3] = {0., 0., 0.}, kb3[3] = {0., 0., 0.};
-  double kb4[3] = {R.k4[0], R.k4[1], R.k4[2]};
-  kfa::acceptVjp(dir, h, g.dtds, s, m, R.pos, R.dir, R.t, posb, dirb, tb, hb, R.dtds, kb1, kb2,
-                 kb3, kb4);
+  kfa::PolyStep ps;
+  kfa::polyPrep(dir, B, ps);
+  kfa::polyCoef(g.qop, h, ps);
+  kfa::PolyOut o;
+  kfa::polyAcceptFwd(pos, dir, t, g.qop, h, g.dtds, g.d37, B, ps, o);
+  // J' = D J
+  kfa::DMat Db;
   kfa::dmZero(Db);
   kfa::JT Jb0;
   kfa::jtZero(Jb0);
-  kfa::jtApplyVjp(D, J0, R.J, Db, Jb0);
-  kfa::transportVjp(dir, g.qop, h, g.d37, B, s, X, Db, dirb, R.qop, hb, R.d37, R.B, kb1, kb2, kb3);
-  kfa::stagesVjp(dir, g.qop, h, B, s, kb1, kb2, kb3, kb4, 0., dirb, R.qop, hb, R.B);
+  kfa::jtApplyVjp(o.D, J0, R.J, Db, Jb0);
+  double posb[3] = {0., 0., 0.}, dirb[3] = {0., 0., 0.}, tb = 0., hb = 0.;
+  kfa::polyAcceptVjp(dir, g.qop, h, g.dtds, g.d37, B, ps, o, R.pos, R.dir, R.t, R.k4, Db, posb,
+                     dirb, tb, R.qop, hb, R.dtds, R.d37, R.B);
   routeStep(R, (int)tr[2 * (T - 1) + 1], hb);
-  // rejected trials, last first: each set the accuracy constraint
+  // rejected trials, last first: each set the accuracy constraint from its
+  // error estimate
   for (int k = T - 2; k >= 0; --k) {
     const double gacc = R.ssAcc;
     R.ssAcc = 0.;
     if (gacc == 0.) continue;
     const double ht = tr[2 * k];
-    kfa::Stages st;
-    kfa::stagesFwd(dir, g.qop, ht, B, st);
+    kfa::polyCoef(g.qop, ht, ps);
     double dsde;
-    const double sc = kfa::accScale(st.err, P.tol, &dsde);
+    const double sc = kfa::accScale(ps.err, P.tol, &dsde);
     double htb = gacc * sc;
-    const double errb = gacc * ht * dsde;
-    double z1[3] = {0., 0., 0.}, z2[3] = {0., 0., 0.}, z3[3] = {0., 0., 0.}, z4[3] = {0., 0., 0.};
-    kfa::stagesVjp(dir, g.qop, ht, B, st, z1, z2, z3, z4, errb, dirb, R.qop, htb, R.B);
+    kfa::polyErrVjp(dir, g.qop, ht, B, ps, gacc * ht * dsde, dirb, R.qop, htb, R.B);
     routeStep(R, (int)tr[2 * k + 1], htb);
   }
   for (int i = 0; i < 3; ++i) {

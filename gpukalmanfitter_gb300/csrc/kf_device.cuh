@@ -38,6 +38,7 @@
 #include <cstdint>
 
 #include "../../include/gb300kf.h"
+#include "kf_adjoint_math.h"
 
 namespace kfd {
 
@@ -421,6 +422,10 @@ __device__ __forceinline__ T rkTrial(const FieldD &F, const T pos[3], const T di
   return (e < T(1e-20)) ? T(1e-20) : e;
 }
 
+template <typename R, typename H>
+__device__ __forceinline__ void applyTransportStep(Lane<R, H> &L, const R DA[3][3], const R DB[3][3],
+                                                   const R Da[3], const R Dc[3], R D37);
+
 // transportMatrix (EigenStepper.ipp:50-124) on its non-zero blocks and
 // jacTransport = D * jacTransport (EigenStepper.ipp:312-318)
 template <typename R, typename H>
@@ -488,7 +493,13 @@ __device__ __forceinline__ void transportUpdate(Lane<R, H> &L, const R dir[3], R
     Da[i] = (h * h) / R(6) * (dk1dL[i] + dk2dL[i] + dk3dL[i]);
     Dc[i] = h6 * (dk1dL[i] + R(2) * (dk2dL[i] + dk3dL[i]) + dk4dL[i]);
   }
-  const R D37 = h * d37;
+  applyTransportStep(L, DA, DB, Da, Dc, h * d37);
+}
+
+// new J = D * J on the structured blocks (EigenStepper.ipp:312-318)
+template <typename R, typename H>
+__device__ __forceinline__ void applyTransportStep(Lane<R, H> &L, const R DA[3][3], const R DB[3][3],
+                                                   const R Da[3], const R Dc[3], R D37) {
   // new J = D * J:
   //  A' = A + DA*B,  a' = a + DA*c + Da,  b' = b + D37,
   //  B' = DB*B,      c' = DB*c + Dc
@@ -520,7 +531,46 @@ template <typename R, typename H> __device__ void rkStep(Lane<R, H> &L, const Pa
   long nTrials = 0;
   double h = ssValue(L);
   if constexpr (sizeof(R) == sizeof(double)) {
-    // ---- plain form: FP64 throughout
+    if (P.field.kind == KF_FIELD_CONSTANT) {
+      // ---- plain form, uniform field: the same RK4 step and transport matrix
+      // through c = d x B and e = c x B (kfa::polyAcceptFwd); the adjoint
+      // differentiates these same formulas
+      kfa::PolyStep w;
+      kfa::polyPrep(L.dir, P.field.B, w);
+      L.hook.stepBegin(L);
+      for (;;) {
+        L.rkTrials++;
+        L.hook.trial(L, h);
+        kfa::polyCoef(L.qop, h, w);
+        if (w.err <= P.tol) break;
+        const double scale = smin(smax(0.25, pow(P.tol / fabs(2. * w.err), 0.25)), 4.);
+        const double hn = h * scale;
+        L.ss[kAccuracy] = hn;
+        L.ssDir = hn > 0. ? 1 : -1;
+        h = ssValue(L);
+        if (h * h < P.cutoff * P.cutoff || nTrials > P.maxTrials) {
+          L.hook.stepEnd(L, false);
+          return;
+        }
+        nTrials++;
+      }
+      L.hook.stepEnd(L, true);
+      kfa::PolyOut o;
+      kfa::polyAcceptFwd(L.pos, L.dir, L.t, L.qop, h, L.dtds, L.d37, P.field.B, w, o);
+      applyTransportStep(L, o.D.DA, o.D.DB, o.D.Da, o.D.Dc, o.D.D37);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        L.pos[i] = o.pos[i];
+        L.dir[i] = o.dir[i];
+        L.k4[i] = o.k4[i];
+      }
+      L.t = o.t;
+      L.stepped = true;
+      L.pathAcc += h;
+      L.rkSteps++;
+      return;
+    }
+    // ---- plain form, field map: FP64 stage by stage
     RkStages<double> s;
     rkFirst<double>(P.field, L.pos, L.dir, L.qop, s);
     L.hook.stepBegin(L);

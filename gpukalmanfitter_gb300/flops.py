@@ -8,6 +8,8 @@ accepted RK steps and the measurement states, so the FLOPs of a batch are
     F = trials*RK_TRIAL + steps*RK_STEP + states*FILTER
         + (states - tracks_fitted)*SMOOTH + tracks*FIXED
 
+with POLY_TRIAL/POLY_STEP in place of RK_TRIAL/RK_STEP in a uniform field.
+
 The dense formulation of the reference (8x8 D*J per step, 8x8*8x6 and 6x8*8x6
 per surface, dense 6x6 products in updater and smoother) would count about
 2.7x more for the same events; DENSE_* give those figures for context.
@@ -17,8 +19,11 @@ from __future__ import annotations
 import numpy as np
 
 # structure-exploiting kernel (what runs on the GPU)
-RK_TRIAL = 94      # one tryRungeKuttaStep: 2 field points, k1..k4, error estimate
-RK_STEP = 591      # accepted step: time, transport matrix blocks, D*J on 25 entries, motion
+RK_TRIAL = 94      # field map: one tryRungeKuttaStep: 2 field points, k1..k4, error estimate
+RK_STEP = 591      # field map: accepted step: time, transport matrix blocks, D*J on 25 entries, motion
+# uniform field: the step through c = d x B, e = c x B (kfa::polyPrep/polyCoef/polyAcceptFwd)
+POLY_TRIAL = 24    # trial coefficients and error estimate
+POLY_STEP = 354    # c, e (23) + motion, k4, D blocks (173) + D*J (139) + path (1) + navigation (18)
 FILTER = 950       # boundState to a plane (J C J^T on the non-zeros) + gain update + reload
 SMOOTH = 652       # one RTS smoother state: structured J^-1 (gain), state, G C G^T
 FIXED = 800        # start state on the perigee line, final transport to the line
@@ -31,8 +36,10 @@ DENSE_SMOOTH = 6 * 6 * 6 * 2 * 4 + 500
 DENSE_FIXED = 2400
 
 
-def batch_flops(n_trials, n_steps, n_meas, status, dense: bool = False) -> float:
-    """FP64 FLOPs of one fit of a batch from the kernel's per-track counters."""
+def batch_flops(n_trials, n_steps, n_meas, status, dense: bool = False,
+                uniform: bool = False) -> float:
+    """FP64 FLOPs of one fit of a batch from the kernel's per-track counters
+    (uniform: the uniform-field step formulation)."""
     t = np.asarray(n_trials, dtype=np.float64).sum()
     s = np.asarray(n_steps, dtype=np.float64).sum()
     m = np.asarray(n_meas, dtype=np.float64)
@@ -41,7 +48,8 @@ def batch_flops(n_trials, n_steps, n_meas, status, dense: bool = False) -> float
     if dense:
         return (t * DENSE_RK_TRIAL + s * DENSE_RK_STEP + m.sum() * DENSE_FILTER
                 + smooth * DENSE_SMOOTH + len(m) * DENSE_FIXED)
-    return t * RK_TRIAL + s * RK_STEP + m.sum() * FILTER + smooth * SMOOTH + len(m) * FIXED
+    trial, step = (POLY_TRIAL, POLY_STEP) if uniform else (RK_TRIAL, RK_STEP)
+    return t * trial + s * step + m.sum() * FILTER + smooth * SMOOTH + len(m) * FIXED
 
 
 def batch_bytes(n_tracks: int, n_surfaces: int) -> dict:

@@ -634,6 +634,80 @@ static double testAlign() {
   return worst;
 }
 
+// the polynomial uniform-field step equals the stage-by-stage step
+static double testPolyEquivalence() {
+  double worst = 0.;
+  for (int t = 0; t < 50; ++t) {
+    double d[3], pos[3] = {100 * N01(), 10 * N01(), N01()}, B[3] = {1e-5 * N01(), 1e-5 * N01(), B0[2]};
+    unitDir(d);
+    const double q = (t % 2 ? 1 : -1) * (0.1 + U01()), h = 5. + 80. * U01(), dtds = 1.001, d37 = 0.01;
+    Stages s;
+    stagesFwd(d, q, h, B, s);
+    Moved m;
+    acceptFwd(pos, d, 0.5, h, dtds, s, m);
+    DMat D;
+    TransportTmp X;
+    transportFwd(d, q, h, d37, B, s, D, X);
+    PolyStep w;
+    polyTrialFwd(d, q, h, B, w);
+    PolyOut o;
+    polyAcceptFwd(pos, d, 0.5, q, h, dtds, d37, B, w, o);
+    auto rel = [](double a, double b, double sc) { return fabs(a - b) / sc; };
+    // the stage-by-stage error estimate carries cancellation noise ~1e-16/x
+    worst = fmax(worst, rel(w.err, s.err, s.err) * 1e-4);
+    for (int i = 0; i < 3; ++i) {
+      worst = fmax(worst, rel(o.pos[i], m.pos[i], 1000.));
+      worst = fmax(worst, rel(o.dir[i], m.dir[i], 1.));
+      worst = fmax(worst, rel(o.k4[i], s.k4[i], fabs(q) * B0[2]));
+      worst = fmax(worst, rel(o.D.Da[i], D.Da[i], h * h * B0[2]));
+      worst = fmax(worst, rel(o.D.Dc[i], D.Dc[i], h * B0[2]));
+      for (int j = 0; j < 3; ++j) {
+        worst = fmax(worst, rel(o.D.DA[i][j], D.DA[i][j], h));
+        worst = fmax(worst, rel(o.D.DB[i][j], D.DB[i][j], 1.));
+      }
+    }
+  }
+  return worst;
+}
+
+static double testPoly() {
+  double worst = 0.;
+  for (int t = 0; t < 20; ++t) {
+    double d[3];
+    unitDir(d);
+    // x: pos 3, d 3, t, q, h, dtds, d37, B 3  (= 14)
+    Vec x = {100 * N01(), 10 * N01(), N01(), d[0], d[1], d[2], 3. * U01(),
+             (t % 2 ? 1 : -1) * (0.1 + U01()), 5. + 60. * U01(), 1. + 0.01 * U01(), 0.01 * N01(),
+             1e-5 * N01(), 1e-5 * N01(), B0[2]};
+    Fn F = [](const Vec &v) {
+      PolyStep w;
+      polyTrialFwd(&v[3], v[7], v[8], &v[11], w);
+      PolyOut o;
+      polyAcceptFwd(&v[0], &v[3], v[6], v[7], v[8], v[9], v[10], &v[11], w, o);
+      Vec y(o.pos, o.pos + 3);
+      y.insert(y.end(), o.dir, o.dir + 3);
+      y.push_back(o.t);
+      y.push_back(w.err);
+      y.insert(y.end(), o.k4, o.k4 + 3);
+      packD(o.D, y);
+      return y;
+    };
+    Vec yb = randv(36);
+    PolyStep w;
+    polyTrialFwd(&x[3], x[7], x[8], &x[11], w);
+    PolyOut o;
+    polyAcceptFwd(&x[0], &x[3], x[6], x[7], x[8], x[9], x[10], &x[11], w, o);
+    DMat Db;
+    unpackD(&yb[11], Db);
+    Vec xb(14, 0.);
+    polyAcceptVjp(&x[3], x[7], x[8], x[9], x[10], &x[11], w, o, &yb[0], &yb[3], yb[6], &yb[8], Db,
+                  &xb[0], &xb[3], xb[6], xb[7], xb[8], xb[9], xb[10], &xb[11]);
+    polyErrVjp(&x[3], x[7], x[8], &x[11], w, yb[7], &xb[3], xb[7], xb[8], &xb[11]);
+    worst = fmax(worst, check(F, x, yb, xb, 1e-5));
+  }
+  return worst;
+}
+
 int main() {
   printf("stages %.3e\n", testStages());
   printf("accept %.3e\n", testAccept());
@@ -648,5 +722,7 @@ int main() {
   printf("smooth %.3e\n", testSmooth());
   printf("start %.3e\n", testStart());
   printf("align %.3e\n", testAlign());
+  printf("polyequiv %.3e\n", testPolyEquivalence());
+  printf("poly %.3e\n", testPoly());
   return 0;
 }
