@@ -149,6 +149,8 @@ struct KalmanFitterOptions {
   bool smoothing = true;
   const LineSurface *referenceSurface = nullptr;
   double outlierChi2Cut = 0.; // 0: no outlier rejection (reference VoidOutlierFinder)
+  bool batched = false;       // fitBatch: length-sorted persistent kernel (batched form)
+  bool mixedPrecision = false; // FP32 propagation and Jacobian transport, FP64 Kalman algebra
 };
 
 struct KalmanFitterResult {
@@ -283,6 +285,8 @@ public:
     cfg.on_surface_tol = m_options.targetTolerance;
     cfg.smoothing = kfOptions.smoothing ? 1 : 0;
     cfg.outlier_chi2_cut = kfOptions.outlierChi2Cut;
+    cfg.kernel = kfOptions.batched ? KF_KERNEL_PERSISTENT : KF_KERNEL_THREAD_PER_TRACK;
+    cfg.precision = kfOptions.mixedPrecision ? KF_PRECISION_MIXED : KF_PRECISION_FP64;
     kf_geometry_t geo{S, 0, center.data(), rot.data()};
     kf_field_t field{};
     field.kind = KF_FIELD_CONSTANT;

@@ -100,6 +100,16 @@ int main() {
   if (!ok) ++bad;
   for (int e = 0; e < 6; ++e)
     if (one.fittedParameters.parameters()[e] != res[7].fittedParameters.parameters()[e]) ++bad;
+  // the batched form (sorted queue, persistent kernel) gives the same fits
+  KalmanFitterOptions bopt = opt;
+  bopt.batched = true;
+  std::vector<KalmanFitterResult> bres;
+  fitter.fitBatch(tracks, bopt, bres, planes.data(), planes.size());
+  for (int64_t i = 0; i < n; ++i) {
+    if (bres[i].status != res[i].status || bres[i].chi2 != res[i].chi2) ++bad;
+    for (int e = 0; e < 6; ++e)
+      if (bres[i].fittedParameters.parameters()[e] != res[i].fittedParameters.parameters()[e]) ++bad;
+  }
   std::printf("shim tracks=%lld mismatches=%d\n", (long long)n, bad);
   return bad == 0 ? 0 : 1;
 }
