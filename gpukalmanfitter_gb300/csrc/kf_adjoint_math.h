@@ -528,13 +528,15 @@ KF_HD void crossMatrix(const double B[3], double A[3][3], double A2[3][3], doubl
 KF_HD void polyAcceptFwd(const double pos[3], const double d[3], double t, double q, double h,
                          double dtds, double d37, const double B[3], const PolyStep &w,
                          PolyOut &o) {
-  const double h6 = h / 6., hh6 = h * h / 6.;
+  // constants as products (a division by a literal is a full FP64 division)
+  const double h6 = h * (1. / 6.), hh6 = h * h6;
   for (int i = 0; i < 3; ++i) {
     o.pos[i] = pos[i] + (h * d[i] + hh6 * (w.P * w.c[i] + w.Q * w.e[i]));
     o.w[i] = d[i] + h6 * (w.Pd * w.c[i] + w.Qd * w.e[i]);
   }
   o.n = sqrt(dot(o.w, o.w));
-  for (int i = 0; i < 3; ++i) o.dir[i] = o.w[i] / o.n;
+  const double in = 1. / o.n;
+  for (int i = 0; i < 3; ++i) o.dir[i] = o.w[i] * in;
   o.t = t + h * dtds;
   const double a4 = q * (1. - 0.5 * w.x), b4 = h * q * q * (1. - 0.25 * w.x);
   for (int i = 0; i < 3; ++i) o.k4[i] = a4 * w.c[i] + b4 * w.e[i];
@@ -608,7 +610,7 @@ KF_HD void polyAcceptVjp(const double d[3], double q, double h, double dtds, dou
                          const double k4b[3], const DMat &Db, double posb[3], double db[3],
                          double &tb, double &qb, double &hb, double &dtdsb, double &d37b,
                          double Bb[3]) {
-  const double h6 = h / 6., hh6 = h * h / 6.;
+  const double h6 = h * (1. / 6.), hh6 = h * h6, h3 = h * (1. / 3.), k6 = 1. / 6.;
   double cb[3] = {0., 0., 0.}, eb[3] = {0., 0., 0.};
   double Pb = 0., Qb = 0., Pdb = 0., Qdb = 0., xb = 0., hqb = 0.;
   // time and D37
@@ -629,7 +631,7 @@ KF_HD void polyAcceptVjp(const double d[3], double q, double h, double dtds, dou
       hc += Db.Dc[i] * w.c[i];
       he += Db.Dc[i] * w.e[i];
     }
-    hb += (h / 3.) * (ea * gc + ebb * ge) + (fa * hc + fbb * he) / 6.;
+    hb += h3 * (ea * gc + ebb * ge) + (fa * hc + fbb * he) * k6;
     xb += hh6 * (-0.75) * gc + h6 * (-3.) * hc + h6 * (-w.hq) * he;
     hqb += hh6 * 2. * ge + h6 * (6. - w.x) * he;
   }
@@ -640,7 +642,7 @@ KF_HD void polyAcceptVjp(const double d[3], double q, double h, double dtds, dou
     const double gA = fro(Db.DA, A), gA2 = fro(Db.DA, A2);
     const double fA = fro(Db.DB, A), fA2 = fro(Db.DB, A2);
     hb += Db.DA[0][0] + Db.DA[1][1] + Db.DA[2][2];
-    hb += (h / 3.) * (w.P * gA + w.Q * gA2) + (w.Pd * fA + w.Qd * fA2) / 6.;
+    hb += h3 * (w.P * gA + w.Q * gA2) + (w.Pd * fA + w.Qd * fA2) * k6;
     Pb += hh6 * gA;
     Qb += hh6 * gA2;
     Pdb += h6 * fA;
@@ -676,7 +678,7 @@ KF_HD void polyAcceptVjp(const double d[3], double q, double h, double dtds, dou
       pe += posb_[i] * w.e[i];
       pd += posb_[i] * d[i];
     }
-    hb += pd + (h / 3.) * (w.P * pc + w.Q * pe);
+    hb += pd + h3 * (w.P * pc + w.Q * pe);
     Pb += hh6 * pc;
     Qb += hh6 * pe;
   }
@@ -685,14 +687,14 @@ KF_HD void polyAcceptVjp(const double d[3], double q, double h, double dtds, dou
     const double pr = dot(o.dir, dirb_);
     double wb[3], wc = 0., we = 0.;
     for (int i = 0; i < 3; ++i) {
-      wb[i] = (dirb_[i] - o.dir[i] * pr) / o.n;
+      wb[i] = (dirb_[i] - o.dir[i] * pr) * (1. / o.n);
       db[i] += wb[i];
       cb[i] += h6 * w.Pd * wb[i];
       eb[i] += h6 * w.Qd * wb[i];
       wc += wb[i] * w.c[i];
       we += wb[i] * w.e[i];
     }
-    hb += (w.Pd * wc + w.Qd * we) / 6.;
+    hb += (w.Pd * wc + w.Qd * we) * k6;
     Pdb += h6 * wc;
     Qdb += h6 * we;
   }

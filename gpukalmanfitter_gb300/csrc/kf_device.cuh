@@ -311,9 +311,10 @@ template <typename R, typename H> __device__ __forceinline__ void ssInit(Lane<R,
 
 // per-leg constants: q/p, dt/ds and the dt/d(q/p) coefficient
 template <typename R, typename H> __device__ __forceinline__ void legConstants(Lane<R, H> &L, double mass) {
-  L.qop = L.q / L.p;
-  L.dtds = hypot(1., mass / L.p);
-  L.d37 = mass * mass * L.q / (L.p * L.dtds);
+  const double ip = 1. / L.p;
+  L.qop = L.q * ip;
+  L.dtds = hypot(1., mass * ip);
+  L.d37 = mass * mass * L.q * ip / L.dtds;
 }
 
 // ---- Jacobian resets -------------------------------------------------------
@@ -828,7 +829,8 @@ __device__ void boundStatePlane(Lane<R, H> &L, const PlaneD &pl, double out[6], 
   // PlaneSurface::derivativeFactors (PlaneSurface.ipp:191-204)
   const R T0 = (R)pl.T[0], T1 = (R)pl.T[1], T2 = (R)pl.T[2];
   const R dp = T0 * (R)L.dir[0] + T1 * (R)L.dir[1] + T2 * (R)L.dir[2];
-  const R nv0 = T0 / dp, nv1 = T1 / dp, nv2 = T2 / dp;
+  const R idp = R(1) / dp;
+  const R nv0 = T0 * idp, nv1 = T1 * idp, nv2 = T2 * idp;
   R sVec[5];
 #pragma unroll
   for (int c = 0; c < 5; ++c) sVec[c] = nv0 * X.Pt[0][c] + nv1 * X.Pt[1][c] + nv2 * X.Pt[2][c];
@@ -893,9 +895,10 @@ __device__ __forceinline__ void stepperUpdate(Lane<R, H> &L, const PlaneD &pl, c
   sincos(par[3], &st, &ct);
   const double d0 = cp * st, d1 = sp * st, d2 = ct;
   const double n = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
-  L.dir[0] = d0 / n;
-  L.dir[1] = d1 / n;
-  L.dir[2] = d2 / n;
+  const double in = 1. / n;
+  L.dir[0] = d0 * in;
+  L.dir[1] = d1 * in;
+  L.dir[2] = d2 * in;
   L.p = fabs(1. / par[4]);
   L.t = par[5];
 #pragma unroll
@@ -930,7 +933,8 @@ __device__ void filterHit(Lane<R, H> &L, const Params &P, const PlaneD *planes, 
   const double S00 = L.cov(0) + v00, S01 = L.cov(1) + v01, S10 = L.cov(1) + v01,
                S11 = L.cov(6) + v11;
   const double det = S00 * S11 - S01 * S10;
-  const double i00 = S11 / det, i01 = -S01 / det, i10 = -S10 / det, i11 = S00 / det;
+  const double idet = 1. / det;
+  const double i00 = S11 * idet, i01 = -S01 * idet, i10 = -S10 * idet, i11 = S00 * idet;
   const double r0 = m0 - pred[0], r1 = m1 - pred[1];
   const double chi2 = r0 * (i00 * r0 + i01 * r1) + r1 * (i10 * r0 + i11 * r1);
   const bool outlier = (P.outlierCut > 0. && chi2 > P.outlierCut);
@@ -1071,41 +1075,42 @@ __device__ __forceinline__ void invJacobian(const T J[25], T Gi[25]) {
 // 5e-8 relative between two valid FP64 evaluations), and without storing
 // covariances per state.
 // ---------------------------------------------------------------------------
-// Mixed-form smoother (no smoothed-state output requested).  The gains
-// G_i = J_i^-1 and the corrections G (x_s' - x_p') are formed in FP32 and
-// added to the FP64 filtered parameters; the smoothed covariance is needed at
-// the first state only, C_s(0) = Pg C_f(n-1) Pg^T with Pg = G_1 ... G_{n-1}
-// accumulated in FP32 on the Jacobian structure.
-template <typename R, typename H>
-__device__ bool finalizeSmoothMixed(Lane<R, H> &L, const Params &P, const PlaneD *planes) {
+// Smoother when no smoothed-state output is requested: only the first
+// state's covariance leaves the fit, C_s(0) = Pg C_f(n-1) Pg^T with
+// Pg = G_1 ... G_{n-1} accumulated on the Jacobian structure (~190 instead of
+// ~470 FLOP per state for G C_s' G^T).  The gains G_i = J_i^-1 and the
+// corrections G (x_s' - x_p') are formed in T (FP32 in the mixed form, FP64
+// in the plain form) and added to the FP64 filtered parameters.
+template <typename T, typename R, typename H>
+__device__ bool finalizeSmoothGain(Lane<R, H> &L, const Params &P, const PlaneD *planes) {
   L.smoothed = true;
   const int n = L.measStates;
   double xs[6];
 #pragma unroll
   for (int e = 0; e < 6; ++e) xs[e] = *wsPtr(P, L, n - 1, 6 + e);
-  float Pg[25];
+  T Pg[25];
 #pragma unroll
-  for (int e = 0; e < 25; ++e) Pg[e] = (e < 20 && e % 6 == 0) ? 1.f : 0.f; // rows 0..3: identity
+  for (int e = 0; e < 25; ++e) Pg[e] = (e < 20 && e % 6 == 0) ? T(1) : T(0); // rows 0..3: identity
   for (int i = n - 2; i >= 0; --i) {
-    float Jn[25], G[25];
+    T Jn[25], G[25];
 #pragma unroll
-    for (int e = 0; e < 25; ++e) Jn[e] = (float)*wsPtr(P, L, i + 1, 12 + e);
-    invJacobian<float>(Jn, G);
+    for (int e = 0; e < 25; ++e) Jn[e] = (T)*wsPtr(P, L, i + 1, 12 + e);
+    invJacobian<T>(Jn, G);
     bool nan = false;
 #pragma unroll
     for (int e = 0; e < 25; ++e) nan = nan || (G[e] != G[e]);
     if (nan) return false;
-    float dx[6];
+    T dx[6];
 #pragma unroll
-    for (int e = 0; e < 6; ++e) dx[e] = (float)(xs[e] - *wsPtr(P, L, i + 1, e));
-    float y[6];
+    for (int e = 0; e < 6; ++e) dx[e] = (T)(xs[e] - *wsPtr(P, L, i + 1, e));
+    T y[6];
 #pragma unroll
     for (int r = 0; r < 6; ++r) {
       if (r == 4) {
         y[4] = dx[4];
       } else {
         const int gr = (r == 5) ? 4 : r;
-        float g = G[5 * gr] * dx[0];
+        T g = G[5 * gr] * dx[0];
 #pragma unroll
         for (int k = 1; k < 5; ++k) g += G[5 * gr + k] * dx[k];
         if (r == 5) g += dx[5];
@@ -1115,12 +1120,12 @@ __device__ bool finalizeSmoothMixed(Lane<R, H> &L, const Params &P, const PlaneD
 #pragma unroll
     for (int e = 0; e < 6; ++e) xs[e] = *wsPtr(P, L, i, 6 + e) + (double)y[e];
     // Pg <- G Pg on the structure [[A, b, 0], [0, 1, 0], [c, d, 1]]
-    float Np[25];
+    T Np[25];
 #pragma unroll
     for (int r = 0; r < 5; ++r) {
 #pragma unroll
       for (int c = 0; c < 5; ++c) {
-        float v = G[5 * r] * Pg[c];
+        T v = G[5 * r] * Pg[c];
 #pragma unroll
         for (int k = 1; k < 4; ++k) v += G[5 * r + k] * Pg[5 * k + c];
         if (c == 4) v += G[5 * r + 4];
@@ -1181,9 +1186,7 @@ __device__ bool finalizeSmoothMixed(Lane<R, H> &L, const Params &P, const PlaneD
 template <typename R, typename H>
 __device__ bool finalizeSmooth(Lane<R, H> &L, const Params &P, const PlaneD *planes) {
   L.smoothed = true;
-  if constexpr (sizeof(R) == sizeof(float)) {
-    if (!P.oSmoothed) return finalizeSmoothMixed(L, P, planes);
-  }
+  if (!P.oSmoothed) return finalizeSmoothGain<R>(L, P, planes);
   const int n = L.measStates;
   double xs[6], Cs[21];
 #pragma unroll
