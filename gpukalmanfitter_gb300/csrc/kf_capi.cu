@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 
 #include "kf_host.h"
 #include "kf_kernels.cuh"
@@ -238,6 +239,90 @@ cudaError_t copyRows(void *dst, size_t dpitchElems, const void *src, size_t spit
   if (!rows || !n) return cudaSuccess;
   return cudaMemcpy2DAsync(dst, dpitchElems * elem, src, spitchElems * elem, n * elem, rows, kind, s);
 }
+
+constexpr int64_t kHostChunkMin = 131072; // tracks per chunk of a pipelined host call
+
+// a second stream per device for the chunk pipeline, created once
+cudaError_t auxStream(cudaStream_t *out) {
+  static std::mutex mu;
+  static cudaStream_t streams[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!streams[dev]) {
+    e = cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      streams[dev] = nullptr;
+      return e;
+    }
+  }
+  *out = streams[dev];
+  return cudaSuccess;
+}
+
+// tracks [c0, c0 + cn) of a host batch: copies in, fit, copies out, on stream
+// s, with staging for cn tracks at d (no synchronisation)
+int32_t hostChunk(const kf_inputs_t *hin, kf_outputs_t *hout, const kf_config_t *cfg,
+                  const kf_geometry_t *geo, const kf_field_t *field, char *d, int64_t c0,
+                  int64_t cn, cudaStream_t s) {
+  const int32_t S = hin->n_surfaces;
+  const bool sm = hout->smoothed != nullptr;
+  const Staging L = stagingLayout(cn, S, sm);
+  const size_t hs = (size_t)hin->stride;
+  cudaError_t e = cudaSuccess;
+  auto chk = [&](cudaError_t x) {
+    if (e == cudaSuccess) e = x;
+  };
+  chk(copyRows(d + L.meas, cn, hin->meas + c0, hs, 8, cn, (size_t)S * 5, cudaMemcpyHostToDevice, s));
+  if (hin->hit_mask)
+    chk(cudaMemcpyAsync(d + L.mask, hin->hit_mask + c0, cn * 8, cudaMemcpyHostToDevice, s));
+  if (hin->n_planes)
+    chk(cudaMemcpyAsync(d + L.nplanes, hin->n_planes + c0, cn * 4, cudaMemcpyHostToDevice, s));
+  chk(copyRows(d + L.start, cn, hin->start_params + c0, hs, 8, cn, 6, cudaMemcpyHostToDevice, s));
+  chk(copyRows(d + L.scov, cn, hin->start_cov + c0, hs, 8, cn, 21, cudaMemcpyHostToDevice, s));
+  chk(copyRows(d + L.perigee, cn, hin->perigee + c0, hs, 8, cn, 3, cudaMemcpyHostToDevice, s));
+  if (e != cudaSuccess) return cudaFail(e, "host-to-device copy");
+  kf_inputs_t din = *hin;
+  din.n_tracks = cn;
+  din.stride = cn;
+  din.meas = reinterpret_cast<const double *>(d + L.meas);
+  din.hit_mask = hin->hit_mask ? reinterpret_cast<const uint64_t *>(d + L.mask) : nullptr;
+  din.n_planes = hin->n_planes ? reinterpret_cast<const int32_t *>(d + L.nplanes) : nullptr;
+  din.start_params = reinterpret_cast<const double *>(d + L.start);
+  din.start_cov = reinterpret_cast<const double *>(d + L.scov);
+  din.perigee = reinterpret_cast<const double *>(d + L.perigee);
+  kf_outputs_t dout;
+  dout.params = reinterpret_cast<double *>(d + L.params);
+  dout.cov = reinterpret_cast<double *>(d + L.cov);
+  dout.chi2 = reinterpret_cast<double *>(d + L.chi2);
+  dout.status = reinterpret_cast<int32_t *>(d + L.status);
+  dout.n_meas = reinterpret_cast<int32_t *>(d + L.nmeas);
+  dout.n_steps = reinterpret_cast<int32_t *>(d + L.nsteps);
+  dout.n_trials = reinterpret_cast<int32_t *>(d + L.ntrials);
+  dout.smoothed = sm ? reinterpret_cast<double *>(d + L.smoothed) : nullptr;
+  const size_t wsb = std::max(wsBytes(cn, S), kf_batch_workspace_size(nullptr, cn, S));
+  const int32_t rc = (cfg->kernel == KF_KERNEL_PERSISTENT)
+                         ? kf_fit_batch_sorted(&din, &dout, cfg, geo, field, d + L.ws, wsb, s)
+                         : kf_fit_batch(&din, &dout, cfg, geo, field, d + L.ws, wsb, s);
+  if (rc) return rc;
+  const size_t os = hs; // host outputs share the input stride
+  chk(copyRows(hout->params + c0, os, dout.params, cn, 8, cn, 6, cudaMemcpyDeviceToHost, s));
+  chk(copyRows(hout->cov + c0, os, dout.cov, cn, 8, cn, 21, cudaMemcpyDeviceToHost, s));
+  chk(cudaMemcpyAsync(hout->chi2 + c0, dout.chi2, cn * 8, cudaMemcpyDeviceToHost, s));
+  chk(cudaMemcpyAsync(hout->status + c0, dout.status, cn * 4, cudaMemcpyDeviceToHost, s));
+  chk(cudaMemcpyAsync(hout->n_meas + c0, dout.n_meas, cn * 4, cudaMemcpyDeviceToHost, s));
+  if (hout->n_steps)
+    chk(cudaMemcpyAsync(hout->n_steps + c0, dout.n_steps, cn * 4, cudaMemcpyDeviceToHost, s));
+  if (hout->n_trials)
+    chk(cudaMemcpyAsync(hout->n_trials + c0, dout.n_trials, cn * 4, cudaMemcpyDeviceToHost, s));
+  if (sm)
+    chk(copyRows(hout->smoothed + c0, os, dout.smoothed, cn, 8, cn, (size_t)S * 27,
+                 cudaMemcpyDeviceToHost, s));
+  if (e != cudaSuccess) return cudaFail(e, "device-to-host copy");
+  return KF_SUCCESS;
+}
 } // namespace
 
 size_t kf_host_staging_size(const kf_config_t *cfg, int64_t n_tracks, int32_t n_surfaces,
@@ -263,51 +348,41 @@ int32_t kf_fit_batch_host(const kf_inputs_t *hin, kf_outputs_t *hout, const kf_c
     return fail(KF_ERR_WORKSPACE_TOO_SMALL, "staging smaller than kf_host_staging_size()%s");
   char *d = static_cast<char *>(dev);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const size_t hs = (size_t)hin->stride;
-  cudaError_t e = cudaSuccess;
-  auto chk = [&](cudaError_t x) {
-    if (e == cudaSuccess) e = x;
-  };
-  chk(copyRows(d + L.meas, n, hin->meas, hs, 8, n, (size_t)S * 5, cudaMemcpyHostToDevice, s));
-  if (hin->hit_mask) chk(cudaMemcpyAsync(d + L.mask, hin->hit_mask, n * 8, cudaMemcpyHostToDevice, s));
-  if (hin->n_planes) chk(cudaMemcpyAsync(d + L.nplanes, hin->n_planes, n * 4, cudaMemcpyHostToDevice, s));
-  chk(copyRows(d + L.start, n, hin->start_params, hs, 8, n, 6, cudaMemcpyHostToDevice, s));
-  chk(copyRows(d + L.scov, n, hin->start_cov, hs, 8, n, 21, cudaMemcpyHostToDevice, s));
-  chk(copyRows(d + L.perigee, n, hin->perigee, hs, 8, n, 3, cudaMemcpyHostToDevice, s));
-  if (e != cudaSuccess) return cudaFail(e, "host-to-device copy");
-  kf_inputs_t din = *hin;
-  din.stride = n;
-  din.meas = reinterpret_cast<const double *>(d + L.meas);
-  din.hit_mask = hin->hit_mask ? reinterpret_cast<const uint64_t *>(d + L.mask) : nullptr;
-  din.n_planes = hin->n_planes ? reinterpret_cast<const int32_t *>(d + L.nplanes) : nullptr;
-  din.start_params = reinterpret_cast<const double *>(d + L.start);
-  din.start_cov = reinterpret_cast<const double *>(d + L.scov);
-  din.perigee = reinterpret_cast<const double *>(d + L.perigee);
-  kf_outputs_t dout;
-  dout.params = reinterpret_cast<double *>(d + L.params);
-  dout.cov = reinterpret_cast<double *>(d + L.cov);
-  dout.chi2 = reinterpret_cast<double *>(d + L.chi2);
-  dout.status = reinterpret_cast<int32_t *>(d + L.status);
-  dout.n_meas = reinterpret_cast<int32_t *>(d + L.nmeas);
-  dout.n_steps = reinterpret_cast<int32_t *>(d + L.nsteps);
-  dout.n_trials = reinterpret_cast<int32_t *>(d + L.ntrials);
-  dout.smoothed = sm ? reinterpret_cast<double *>(d + L.smoothed) : nullptr;
-  const size_t wsb = std::max(wsBytes(n, S), kf_batch_workspace_size(nullptr, n, S));
-  rc = (cfg->kernel == KF_KERNEL_PERSISTENT)
-           ? kf_fit_batch_sorted(&din, &dout, cfg, geo, field, d + L.ws, wsb, stream)
-           : kf_fit_batch(&din, &dout, cfg, geo, field, d + L.ws, wsb, stream);
-  if (rc) return rc;
-  const size_t os = (size_t)hin->stride; // host outputs share the input stride
-  chk(copyRows(hout->params, os, dout.params, n, 8, n, 6, cudaMemcpyDeviceToHost, s));
-  chk(copyRows(hout->cov, os, dout.cov, n, 8, n, 21, cudaMemcpyDeviceToHost, s));
-  chk(cudaMemcpyAsync(hout->chi2, dout.chi2, n * 8, cudaMemcpyDeviceToHost, s));
-  chk(cudaMemcpyAsync(hout->status, dout.status, n * 4, cudaMemcpyDeviceToHost, s));
-  chk(cudaMemcpyAsync(hout->n_meas, dout.n_meas, n * 4, cudaMemcpyDeviceToHost, s));
-  if (hout->n_steps) chk(cudaMemcpyAsync(hout->n_steps, dout.n_steps, n * 4, cudaMemcpyDeviceToHost, s));
-  if (hout->n_trials) chk(cudaMemcpyAsync(hout->n_trials, dout.n_trials, n * 4, cudaMemcpyDeviceToHost, s));
-  if (sm) chk(copyRows(hout->smoothed, os, dout.smoothed, n, 8, n, (size_t)S * 27, cudaMemcpyDeviceToHost, s));
-  if (e != cudaSuccess) return cudaFail(e, "device-to-host copy");
-  e = cudaStreamSynchronize(s);
+  // Large batches run as K chunks alternating between the caller's stream and
+  // a second stream of this device, so that one chunk's copies overlap
+  // another chunk's fit; two staging slots of chunk size fit in the staging
+  // area sized for the whole batch.
+  int K = n >= 4 * kHostChunkMin ? 4 : (n >= 2 * kHostChunkMin ? 2 : 1);
+  const int64_t chunk = (n + K - 1) / K;
+  const size_t slot = stagingLayout(chunk, S, sm).total;
+  cudaStream_t aux = nullptr;
+  if (K > 1 && (2 * slot > bytes || auxStream(&aux) != cudaSuccess)) K = 1;
+  if (K == 1) {
+    rc = hostChunk(hin, hout, cfg, geo, field, d, 0, n, s);
+    if (rc) return rc;
+  } else {
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaError_t e = cudaEventCreateWithFlags(&ev0, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev1, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(ev0, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(aux, ev0, 0);
+    if (e != cudaSuccess) return cudaFail(e, "chunk pipeline set-up");
+    for (int k = 0; k < K && rc == KF_SUCCESS; ++k) {
+      const int64_t c0 = k * chunk, cn = std::min(chunk, n - c0);
+      if (cn <= 0) break;
+      rc = hostChunk(hin, hout, cfg, geo, field, d + (k % 2) * slot, c0, cn, (k % 2) ? aux : s);
+    }
+    // the caller's stream continues after both streams' work
+    e = cudaEventRecord(ev1, aux);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ev1, 0);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cudaFail(e, "chunk pipeline");
+    return KF_SUCCESS;
+  }
+  cudaError_t e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cudaFail(e, "stream synchronize");
   return KF_SUCCESS;
 }

@@ -194,8 +194,11 @@ size_t kf_host_staging_size(const kf_config_t *cfg, int64_t n_tracks,
                             int32_t n_surfaces, int32_t with_smoothed);
 
 /* Fit a batch held in HOST memory (pinned memory gives async copies): copies
- * inputs into `device_staging`, fits, copies the outputs back, all on
- * `stream`.  Blocks until the results are on the host. */
+ * inputs into `device_staging`, fits, copies the outputs back, and blocks
+ * until the results are on the host.  Batches of 262144 tracks or more run as
+ * 2 or 4 chunks alternating between `stream` and a second stream the library
+ * keeps per device, so that the copies of one chunk overlap the fit of
+ * another (with pinned host memory); results are the same as one chunk's. */
 int32_t kf_fit_batch_host(const kf_inputs_t *host_in, kf_outputs_t *host_out,
                           const kf_config_t *cfg, const kf_geometry_t *geo,
                           const kf_field_t *field, void *device_staging,

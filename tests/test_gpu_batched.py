@@ -125,3 +125,21 @@ def test_sorted_small_batches(kf, n):
     ref = b.results()
     b.fit_sorted()
     _same(b.results(), ref)
+
+
+@pytest.mark.parametrize("kernel", [1, 2])
+def test_host_call_pipelined_in_chunks(kf, kernel):
+    """kf_fit_batch_host splits large batches into chunks on two streams: the
+    results equal the device-buffer call's."""
+    import torch
+    tel = kf.make_telescope(300_000, seed=23)  # two chunks
+    cfg = kf.default_config(overstep_limit=0.1, kernel=kernel)
+    b = kf.DeviceBatch(tel, cfg)
+    if kernel == 2:
+        b.fit_sorted()
+    else:
+        b.fit()
+    ref = b.results()
+    h = kf.fit_host(tel, cfg)
+    torch.cuda.synchronize()
+    _same(h, ref)
