@@ -216,12 +216,12 @@ def timed_steps(step, stream, steps: int, warmup: int, barrier) -> tuple:
     return t_start.elapsed_time(t_end), [a.elapsed_time(b) for a, b in evs]
 
 
-def batched_step(batch, stream, ctas_per_sm: int = 0) -> tuple:
+def batched_step(batch, stream, ctas_per_sm: int = 0, block_size: int = 128) -> tuple:
     """Autotune the persistent kernel shape on this batch (or take the given
-    CTAs per SM), capture the sort and the fit into a CUDA graph; one step =
-    one graph launch (4 kernels)."""
+    threads per CTA and CTAs per SM), capture the sort and the fit into a CUDA
+    graph; one step = one graph launch (4 kernels)."""
     if ctas_per_sm:
-        batch.cfg.block_size, batch.cfg.min_blocks_per_sm = 128, ctas_per_sm
+        batch.cfg.block_size, batch.cfg.min_blocks_per_sm = block_size, ctas_per_sm
         batch.cfg.kernel = 2
         tuned, tune_ms = batch.cfg, 0.0
     else:
@@ -335,7 +335,7 @@ def run_gpu(args) -> None:
     torch.cuda.synchronize()
     shape = None
     if args.form == "batched":
-        step, per_step, shape = batched_step(batch, stream, args.ctas_per_sm)
+        step, per_step, shape = batched_step(batch, stream, args.ctas_per_sm, args.block_size)
     else:
         step, per_step = (lambda: batch.fit(stream)), 1
 
@@ -451,7 +451,7 @@ def traffic_estimate(args, n: int, shape):
         return None
     key = f"{args.workload}/{args.precision}/{args.form}"
     if shape:
-        key += f"/ctas{shape['ctas_per_sm']}"
+        key += f"/{shape['threads_per_cta']}x{shape['ctas_per_sm']}"
     try:
         rec = json.loads(tfile.read_text()).get(key)
         return rec["dram_bytes_per_track"] * n if rec else None
@@ -544,8 +544,11 @@ def main() -> None:
                          "plain: one thread per track, grid over the batch")
     ap.add_argument("--no-suite", action="store_true",
                     help="skip the uneven-track, field-map and adjoint comparisons")
-    ap.add_argument("--ctas-per-sm", type=int, default=0, choices=[0, 2, 3, 4, 5],
-                    help="batched form: persistent kernel shape (0 = autotune)")
+    ap.add_argument("--ctas-per-sm", type=int, default=0, choices=[0, 1, 2, 3, 4, 5, 8],
+                    help="batched form: persistent kernel CTAs per SM (0 = autotune)")
+    ap.add_argument("--block-size", type=int, default=128, choices=[64, 128, 256],
+                    help="batched form with --ctas-per-sm: threads per CTA; compiled "
+                         "shapes 128 x 2..5, 64 x 4, 64 x 8, 256 x 1, 256 x 2")
     ap.add_argument("--suite", default="batching,precision_map,differentiation",
                     help="comma list of suite entries to run (or 'none')")
     args = ap.parse_args()

@@ -21,31 +21,67 @@
 using namespace kfd;
 using namespace kfh;
 
-// persistent-kernel instantiations (kf_fit_*.cu, kf_tune_*.cu)
-cudaError_t launchPersistent_fp64_128_2(const kfd::Params &, cudaStream_t);
-cudaError_t launchPersistent_fp64_128_3(const kfd::Params &, cudaStream_t);
+// persistent-kernel instantiations (kf_fit_*.cu, kf_tune_*.cu): launcher and
+// shared-memory set-up
 cudaError_t launchPersistent_fp64_128_4(const kfd::Params &, cudaStream_t);
+cudaError_t launchPersistent_fp64_128_4_prep();
+cudaError_t launchPersistent_fp64_128_2(const kfd::Params &, cudaStream_t);
+cudaError_t launchPersistent_fp64_128_2_prep();
+cudaError_t launchPersistent_fp64_128_3(const kfd::Params &, cudaStream_t);
+cudaError_t launchPersistent_fp64_128_3_prep();
 cudaError_t launchPersistent_fp64_128_5(const kfd::Params &, cudaStream_t);
-cudaError_t launchPersistent_mixed_128_2(const kfd::Params &, cudaStream_t);
-cudaError_t launchPersistent_mixed_128_3(const kfd::Params &, cudaStream_t);
+cudaError_t launchPersistent_fp64_128_5_prep();
+cudaError_t launchPersistent_fp64_64_4(const kfd::Params &, cudaStream_t);
+cudaError_t launchPersistent_fp64_64_4_prep();
+cudaError_t launchPersistent_fp64_64_8(const kfd::Params &, cudaStream_t);
+cudaError_t launchPersistent_fp64_64_8_prep();
+cudaError_t launchPersistent_fp64_256_1(const kfd::Params &, cudaStream_t);
+cudaError_t launchPersistent_fp64_256_1_prep();
+cudaError_t launchPersistent_fp64_256_2(const kfd::Params &, cudaStream_t);
+cudaError_t launchPersistent_fp64_256_2_prep();
 cudaError_t launchPersistent_mixed_128_4(const kfd::Params &, cudaStream_t);
+cudaError_t launchPersistent_mixed_128_4_prep();
+cudaError_t launchPersistent_mixed_128_2(const kfd::Params &, cudaStream_t);
+cudaError_t launchPersistent_mixed_128_2_prep();
+cudaError_t launchPersistent_mixed_128_3(const kfd::Params &, cudaStream_t);
+cudaError_t launchPersistent_mixed_128_3_prep();
 cudaError_t launchPersistent_mixed_128_5(const kfd::Params &, cudaStream_t);
+cudaError_t launchPersistent_mixed_128_5_prep();
+cudaError_t launchPersistent_mixed_64_4(const kfd::Params &, cudaStream_t);
+cudaError_t launchPersistent_mixed_64_4_prep();
+cudaError_t launchPersistent_mixed_64_8(const kfd::Params &, cudaStream_t);
+cudaError_t launchPersistent_mixed_64_8_prep();
+cudaError_t launchPersistent_mixed_256_1(const kfd::Params &, cudaStream_t);
+cudaError_t launchPersistent_mixed_256_1_prep();
+cudaError_t launchPersistent_mixed_256_2(const kfd::Params &, cudaStream_t);
+cudaError_t launchPersistent_mixed_256_2_prep();
 
 namespace {
 
 struct Variant {
   int precision, bs, minb;
   cudaError_t (*launch)(const Params &, cudaStream_t);
+  cudaError_t (*prep)();
 };
+// (threads per CTA, CTAs per SM): register budgets 255 (128x2, 64x4, 256x1),
+// 168 (128x3), 128 (128x4, 64x8, 256x2), 96 (128x5)
 const Variant kVariants[] = {
-    {KF_PRECISION_FP64, 128, 4, launchPersistent_fp64_128_4},
-    {KF_PRECISION_FP64, 128, 2, launchPersistent_fp64_128_2},
-    {KF_PRECISION_FP64, 128, 3, launchPersistent_fp64_128_3},
-    {KF_PRECISION_FP64, 128, 5, launchPersistent_fp64_128_5},
-    {KF_PRECISION_MIXED, 128, 4, launchPersistent_mixed_128_4},
-    {KF_PRECISION_MIXED, 128, 2, launchPersistent_mixed_128_2},
-    {KF_PRECISION_MIXED, 128, 3, launchPersistent_mixed_128_3},
-    {KF_PRECISION_MIXED, 128, 5, launchPersistent_mixed_128_5},
+    {KF_PRECISION_FP64, 128, 4, launchPersistent_fp64_128_4, launchPersistent_fp64_128_4_prep},
+    {KF_PRECISION_FP64, 128, 2, launchPersistent_fp64_128_2, launchPersistent_fp64_128_2_prep},
+    {KF_PRECISION_FP64, 128, 3, launchPersistent_fp64_128_3, launchPersistent_fp64_128_3_prep},
+    {KF_PRECISION_FP64, 128, 5, launchPersistent_fp64_128_5, launchPersistent_fp64_128_5_prep},
+    {KF_PRECISION_FP64, 64, 4, launchPersistent_fp64_64_4, launchPersistent_fp64_64_4_prep},
+    {KF_PRECISION_FP64, 64, 8, launchPersistent_fp64_64_8, launchPersistent_fp64_64_8_prep},
+    {KF_PRECISION_FP64, 256, 1, launchPersistent_fp64_256_1, launchPersistent_fp64_256_1_prep},
+    {KF_PRECISION_FP64, 256, 2, launchPersistent_fp64_256_2, launchPersistent_fp64_256_2_prep},
+    {KF_PRECISION_MIXED, 128, 4, launchPersistent_mixed_128_4, launchPersistent_mixed_128_4_prep},
+    {KF_PRECISION_MIXED, 128, 2, launchPersistent_mixed_128_2, launchPersistent_mixed_128_2_prep},
+    {KF_PRECISION_MIXED, 128, 3, launchPersistent_mixed_128_3, launchPersistent_mixed_128_3_prep},
+    {KF_PRECISION_MIXED, 128, 5, launchPersistent_mixed_128_5, launchPersistent_mixed_128_5_prep},
+    {KF_PRECISION_MIXED, 64, 4, launchPersistent_mixed_64_4, launchPersistent_mixed_64_4_prep},
+    {KF_PRECISION_MIXED, 64, 8, launchPersistent_mixed_64_8, launchPersistent_mixed_64_8_prep},
+    {KF_PRECISION_MIXED, 256, 1, launchPersistent_mixed_256_1, launchPersistent_mixed_256_1_prep},
+    {KF_PRECISION_MIXED, 256, 2, launchPersistent_mixed_256_2, launchPersistent_mixed_256_2_prep},
 };
 
 // the instantiation for a configuration (block size 0/128, min blocks 0 = 4)
@@ -154,6 +190,10 @@ int32_t prepare(const kf_inputs_t *in, kf_outputs_t *out, const kf_config_t *cfg
   if (in->n_tracks > 0x7f000000LL) return fail(KF_ERR_INVALID_ARGUMENT, "batch above 2^31 - 2^24 tracks%s");
   v = findVariant(cfg);
   if (!v) return fail(KF_ERR_UNSUPPORTED, "no persistent kernel for this block size / CTAs per SM%s");
+  {
+    const cudaError_t e = v->prep();
+    if (e != cudaSuccess) return cudaFail(e, "persistent kernel shared-memory set-up");
+  }
   L = batchLayout(in->n_tracks, in->n_surfaces);
   if (in->n_tracks > 0 && (!workspace || bytes < L.total))
     return fail(KF_ERR_WORKSPACE_TOO_SMALL, "workspace smaller than kf_batch_workspace_size()%s");

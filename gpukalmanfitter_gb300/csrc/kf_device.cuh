@@ -195,20 +195,14 @@ __device__ __forceinline__ void getField(const FieldD &F, const float p[3], floa
 // smoother, final transport), never in the stepping loop.  They live in
 // dynamic shared memory, one column per thread ([element][thread]: a warp's
 // 32 lanes touch 32 consecutive words, no bank conflicts), so that the
-// stepping loop's register set stays small.  Every fit kernel runs
-// kLaneSlots threads per CTA.
+// stepping loop's register set stays small.  Layout for a CTA of n threads:
+// cov [21][n] double, then g03 [12][n] and g46 [6][n] in R.
 // ---------------------------------------------------------------------------
-constexpr int kLaneSlots = 128;
-template <typename R> struct ColdState {
-  double cov[21][kLaneSlots]; // bound covariance, upper triangle
-  R g03[12][kLaneSlots];      // jacToGlobal rows 0-2, cols 0-3
-  R g46[6][kLaneSlots];       // jacToGlobal rows 4-6, cols 2-3
-};
+constexpr int kLaneSlots = 128; // threads per CTA of the grid form and the adjoint
 extern __shared__ __align__(16) unsigned char kfColdSmem[];
-template <typename R> __device__ __forceinline__ ColdState<R> &coldState() {
-  return *reinterpret_cast<ColdState<R> *>(kfColdSmem);
+template <typename R> __host__ __device__ constexpr size_t coldStateBytes(int threads = kLaneSlots) {
+  return (size_t)threads * (21 * sizeof(double) + 18 * sizeof(R));
 }
-template <typename R> constexpr size_t coldStateBytes() { return sizeof(ColdState<R>); }
 
 // Recording hook of a lane: the fit kernels use NoHook (every call compiles
 // to nothing); the chi2 adjoint records its tape through these calls.
@@ -232,10 +226,17 @@ template <typename R, typename H = NoHook> struct Lane {
   R JA[3][3], Ja[3], Jb, JB[3][3], Jc[3]; // transport Jacobian blocks
   R k4[3];     // k4 of the last step (derivative rows 4..6)
   bool stepped; // a step since the last Jacobian reset (else derivative = 0)
-  // cold state (shared memory, see ColdState)
-  __device__ __forceinline__ double &cov(int e) const { return coldState<R>().cov[e][threadIdx.x]; }
-  __device__ __forceinline__ R &g03(int r, int c) const { return coldState<R>().g03[r * 4 + c][threadIdx.x]; }
-  __device__ __forceinline__ R &g46(int r, int c) const { return coldState<R>().g46[r * 2 + c][threadIdx.x]; }
+  // cold state (shared memory, see coldStateBytes)
+  __device__ __forceinline__ double &cov(int e) const {
+    return reinterpret_cast<double *>(kfColdSmem)[e * blockDim.x + threadIdx.x];
+  }
+  __device__ __forceinline__ R &g03(int r, int c) const {
+    return reinterpret_cast<R *>(kfColdSmem + 21 * sizeof(double) * blockDim.x)[(r * 4 + c) * blockDim.x + threadIdx.x];
+  }
+  __device__ __forceinline__ R &g46(int r, int c) const {
+    return reinterpret_cast<R *>(kfColdSmem + (21 * sizeof(double) + 12 * sizeof(R)) * blockDim.x)
+        [(r * 2 + c) * blockDim.x + threadIdx.x];
+  }
   // per-leg constants (functions of p only)
   double qop, dtds, d37;
   // ---- navigation / actor

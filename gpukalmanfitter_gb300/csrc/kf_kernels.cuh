@@ -54,14 +54,8 @@ __device__ __forceinline__ void fitWarp(const Params &P, const PlaneD *sp, int64
   }
 }
 
-// Static shared memory (surface table) plus the dynamic cold state must stay
-// within the 48 KB a CTA gets without an opt-in.
-static_assert(sizeof(PlaneD) * KF_MAX_PLANES + sizeof(ColdState<double>) <= 48 * 1024,
-              "fit kernel shared memory above 48 KB");
-
 template <int BS, int MINB, typename R>
 __global__ void __launch_bounds__(BS, MINB) fitGrid(const __grid_constant__ Params P) {
-  static_assert(BS == kLaneSlots, "cold state holds kLaneSlots columns");
   __shared__ PlaneD sp[KF_MAX_PLANES];
   for (int k = threadIdx.x; k < P.nSurf; k += BS) sp[k] = P.planes[k];
   __syncthreads();
@@ -71,7 +65,6 @@ __global__ void __launch_bounds__(BS, MINB) fitGrid(const __grid_constant__ Para
 
 template <int BS, int MINB, typename R>
 __global__ void __launch_bounds__(BS, MINB) fitPersistent(const __grid_constant__ Params P) {
-  static_assert(BS == kLaneSlots, "cold state holds kLaneSlots columns");
   __shared__ PlaneD sp[KF_MAX_PLANES];
   for (int k = threadIdx.x; k < P.nSurf; k += BS) sp[k] = P.planes[k];
   __syncthreads();
@@ -91,7 +84,14 @@ __global__ void __launch_bounds__(BS, MINB) fitPersistent(const __grid_constant_
 
 // Launcher of one instantiation of the persistent kernel: as many CTAs as the
 // device holds at once (occupancy query), never more than the batch needs.
+// NAME##_prep lifts the CTA's dynamic shared-memory limit to the cold state's
+// size (needed above 48 KB); callers run it before any launch or capture.
 #define KF_PERSISTENT_LAUNCHER(NAME, BS, MINB, R)                                              \
+  cudaError_t NAME##_prep() {                                                                \
+    return cudaFuncSetAttribute(kfd::fitPersistent<BS, MINB, R>,                             \
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,                 \
+                                (int)kfd::coldStateBytes<R>(BS));                            \
+  }                                                                                          \
   cudaError_t NAME(const kfd::Params &P, cudaStream_t s) {                                   \
     int dev = 0, sms = 0, per = 0;                                                           \
     cudaError_t e = cudaGetDevice(&dev);                                                     \
@@ -99,12 +99,12 @@ __global__ void __launch_bounds__(BS, MINB) fitPersistent(const __grid_constant_
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);                   \
     if (e != cudaSuccess) return e;                                                          \
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kfd::fitPersistent<BS, MINB, R>, \
-                                                      BS, kfd::coldStateBytes<R>());         \
+                                                      BS, kfd::coldStateBytes<R>(BS));       \
     if (e != cudaSuccess) return e;                                                          \
     int64_t blocks = (int64_t)sms * (per > 0 ? per : 1);                                     \
     const int64_t need = (P.n + BS - 1) / BS;                                                \
     if (blocks > need) blocks = need;                                                        \
     if (blocks < 1) blocks = 1;                                                              \
-    kfd::fitPersistent<BS, MINB, R><<<(unsigned)blocks, BS, kfd::coldStateBytes<R>(), s>>>(P); \
+    kfd::fitPersistent<BS, MINB, R><<<(unsigned)blocks, BS, kfd::coldStateBytes<R>(BS), s>>>(P); \
     return cudaGetLastError();                                                               \
   }

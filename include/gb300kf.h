@@ -108,10 +108,13 @@ typedef struct kf_config {
                                 form for KF_KERNEL_PERSISTENT and the
                                 thread-per-track grid otherwise; the device-buffer
                                 entry points each run their own form */
-  int32_t block_size;        /* batched form: threads per CTA, 0 = 128 */
+  int32_t block_size;        /* batched form: threads per CTA (64, 128, 256),
+                                0 = 128 */
   int32_t min_blocks_per_sm; /* batched form: CTAs per SM the persistent kernel
                                 is compiled for (its register budget), 0 = 4;
-                                kf_autotune picks it */
+                                compiled shapes (threads x CTAs): 128 x 2..5,
+                                64 x 4, 64 x 8, 256 x 1, 256 x 2; kf_autotune
+                                picks one */
 } kf_config_t;
 
 /* The surface sequence: boundless plane surfaces (PlaneSurface<InfiniteBounds>,
@@ -232,8 +235,8 @@ int32_t kf_batch_plan_create(kf_batch_plan_t **plan, const kf_inputs_t *in,
 int32_t kf_batch_plan_launch(kf_batch_plan_t *plan, void *stream);
 void kf_batch_plan_destroy(kf_batch_plan_t *plan);
 
-/* Times every compiled persistent-kernel shape (CTAs per SM 2..5 at 128
- * threads) of cfg->precision on the first min(n, 524288) tracks of the batch
+/* Times every compiled persistent-kernel shape (threads per CTA and CTAs per
+ * SM, see kf_config_t.min_blocks_per_sm) of cfg->precision on the first min(n, 524288) tracks of the batch
  * (best of three runs after a warm-up) and returns the fastest configuration
  * in *tuned (and its time per fit of the sample in *best_ms).  Overwrites
  * the outputs of those tracks.  Shapes differ in register allocation only;

@@ -8,6 +8,8 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 KEYS = ("params", "cov", "chi2", "status", "n_meas", "n_steps", "n_trials")
+# compiled persistent-kernel shapes: (threads per CTA, CTAs per SM)
+SHAPES = [(128, 2), (128, 3), (128, 4), (128, 5), (64, 4), (64, 8), (256, 1), (256, 2)]
 
 
 def _same(a, b):
@@ -83,7 +85,7 @@ def test_autotune_picks_a_compiled_shape(kf):
     b.fit()
     ref = b.results()
     tuned, ms = b.autotune()
-    assert tuned.block_size == 128 and tuned.min_blocks_per_sm in (2, 3, 4, 5) and ms > 0
+    assert (tuned.block_size, tuned.min_blocks_per_sm) in SHAPES and ms > 0
     assert tuned.precision == cfg.precision and tuned.outlier_chi2_cut == 25.0
     b.fit_sorted()
     g = b.results()
@@ -96,11 +98,12 @@ def test_autotune_picks_a_compiled_shape(kf):
 
 
 @pytest.mark.parametrize("precision", [0, 1])
-@pytest.mark.parametrize("minb", [2, 3, 4, 5])
-def test_every_compiled_shape_runs(kf, precision, minb):
-    tel = _holes(kf, 8_000, seed=minb)
+@pytest.mark.parametrize("shape", SHAPES)
+def test_every_compiled_shape_runs(kf, precision, shape):
+    bs, minb = shape
+    tel = _holes(kf, 8_000, seed=minb + bs)
     cfg = kf.default_config(overstep_limit=0.1, outlier_chi2_cut=25.0, precision=precision,
-                            min_blocks_per_sm=minb, block_size=128)
+                            min_blocks_per_sm=minb, block_size=bs)
     b = kf.DeviceBatch(tel, cfg)
     b.fit()
     ref = b.results()
