@@ -115,10 +115,13 @@ void fillParams(Params &P, const kf_inputs_t *in, const kf_outputs_t *out, const
   F.grid = reinterpret_cast<const float4 *>(field->grid);
   for (int a = 0; a < 3; ++a) {
     F.Bf[a] = (float)F.B[a];
+    F.Blo[a] = (float)(F.B[a] - (double)F.Bf[a]);
     F.mnf[a] = (float)F.mn[a];
     F.invwf[a] = (float)F.invw[a];
+    F.wf[a] = field->kind == KF_FIELD_GRID3D ? (float)(1. / F.invw[a]) : 0.f;
   }
   F.scalef = (float)F.scale;
+  F.scalelo = (float)(F.scale - (double)F.scalef);
   P.tolLoF = (float)(P.tol * 0.99);
   P.tolHiF = (float)(P.tol * 1.01);
   for (int k = 0; k < in->n_surfaces; ++k) {

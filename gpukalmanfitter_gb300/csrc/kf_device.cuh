@@ -24,9 +24,10 @@
 //
 // Precision.  Lane<R> carries the transport Jacobians in R.  R = double is
 // the plain form (FP64 throughout).  R = float is the mixed form: field
-// interpolation, RK4 stages, the error estimate, the transport matrix and all
-// Jacobians in FP32; position, direction, time, step sizes, covariance, gain
-// (Joseph-form update) and smoother in FP64.  The mixed form accepts or
+// interpolation in FP32 on differences from a cell corner, RK4 stages k2..k4
+// as FP32 offsets from an FP64 k1, the error estimate, the transport matrix
+// and all Jacobians in FP32; position, direction, time, step sizes,
+// covariance, gain (Joseph-form update) and smoother in FP64.  The mixed form accepts or
 // rejects an RK trial on its FP32 error estimate unless that estimate lies
 // within 1 % of the tolerance, where the trial is re-evaluated in FP64, so
 // its step sequence follows the FP64 fit's.
@@ -39,6 +40,7 @@
 
 #include "../../include/gb300kf.h"
 #include "kf_adjoint_math.h"
+#include "kf_ff.cuh"
 
 namespace kfd {
 
@@ -61,6 +63,7 @@ struct FieldD {
   double mn[3], invw[3];
   const float4 *grid;
   float Bf[3], mnf[3], invwf[3], scalef; // FP32 copies for the mixed form
+  float Blo[3], wf[3], scalelo;          // mixed form: lo parts of B and scale, cell width
 };
 
 struct Params {
@@ -106,7 +109,7 @@ enum { PC_PRE = 0, PC_LOOP = 1, PC_ACT = 2, PC_POST = 3, PC_DONE = 4 };
 // ---------------------------------------------------------------------------
 // Magnetic field lookup: Test::ConstantBField (Test/Helper.hpp:17-22) or the
 // trilinear map (MagneticField/InterpolatedBFieldMap.hpp:178-181), in FP64
-// (plain form) or FP32 (mixed form).
+// (plain form) or FP32 pairs (mixed form, getFieldFF).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void getField(const FieldD &F, const double p[3], double B[3]) {
   if (F.kind == KF_FIELD_CONSTANT) {
@@ -147,22 +150,28 @@ __device__ __forceinline__ void getField(const FieldD &F, const double p[3], dou
   B[2] = tri(v000.z, v100.z, v010.z, v110.z, v001.z, v101.z, v011.z, v111.z);
 }
 
-__device__ __forceinline__ void getField(const FieldD &F, const float p[3], float B[3]) {
+// Mixed form: the field as float pairs (kf_ff.cuh).  The cell is found from
+// the FP32 position; the weights are taken from the offset to the cell's
+// lower corner, p - (min + i w), which is exact for a float-representable
+// grid, so they carry no error from the position's magnitude.  The trilinear
+// interpolation runs in FP32 on the corner values' differences from the
+// lower corner, v - v000, and adds v000 back as a pair: its rounding errors
+// scale with the field's variation across the cell, not with the field.
+__device__ __forceinline__ void getFieldFF(const FieldD &F, const float p[3], kff::ff B[3]) {
   if (F.kind == KF_FIELD_CONSTANT) {
-    B[0] = F.Bf[0];
-    B[1] = F.Bf[1];
-    B[2] = F.Bf[2];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) B[a] = {F.Bf[a], F.Blo[a]};
     return;
   }
   int idx[3];
   float f[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    float g = (p[a] - F.mnf[a]) * F.invwf[a];
+    const float g = (p[a] - F.mnf[a]) * F.invwf[a];
     int i = (int)floorf(g);
     i = min(max(i, 0), F.n[a] - 2);
     idx[a] = i;
-    f[a] = g - (float)i;
+    f[a] = __fmul_rn(__fsub_rn(p[a], __fmaf_rn((float)i, F.wf[a], F.mnf[a])), F.invwf[a]);
   }
   const size_t nx = F.n[0], nxy = (size_t)F.n[0] * F.n[1];
   const size_t base = (size_t)idx[2] * nxy + (size_t)idx[1] * nx + idx[0];
@@ -170,16 +179,17 @@ __device__ __forceinline__ void getField(const FieldD &F, const float p[3], floa
   const float4 v010 = __ldg(F.grid + base + nx), v110 = __ldg(F.grid + base + nx + 1);
   const float4 v001 = __ldg(F.grid + base + nxy), v101 = __ldg(F.grid + base + nxy + 1);
   const float4 v011 = __ldg(F.grid + base + nxy + nx), v111 = __ldg(F.grid + base + nxy + nx + 1);
-  const float sc = F.scalef;
+  const kff::ff sc = {F.scalef, F.scalelo};
   auto tri = [&](float a000, float a100, float a010, float a110, float a001, float a101,
                  float a011, float a111) {
-    float c00 = a000 + f[0] * (a100 - a000);
-    float c10 = a010 + f[0] * (a110 - a010);
-    float c01 = a001 + f[0] * (a101 - a001);
-    float c11 = a011 + f[0] * (a111 - a011);
-    float c0 = c00 + f[1] * (c10 - c00);
-    float c1 = c01 + f[1] * (c11 - c01);
-    return (c0 + f[2] * (c1 - c0)) * sc;
+    const float d010 = a010 - a000, d001 = a001 - a000, d011 = a011 - a000;
+    const float c00 = f[0] * (a100 - a000);
+    const float c10 = d010 + f[0] * ((a110 - a000) - d010);
+    const float c01 = d001 + f[0] * ((a101 - a000) - d001);
+    const float c11 = d011 + f[0] * ((a111 - a000) - d011);
+    const float c0 = c00 + f[1] * (c10 - c00);
+    const float c1 = c01 + f[1] * (c11 - c01);
+    return kff::mul(kff::twoSum(a000, c0 + f[2] * (c1 - c0)), sc);
   };
   B[0] = tri(v000.x, v100.x, v010.x, v110.x, v001.x, v101.x, v011.x, v111.x);
   B[1] = tri(v000.y, v100.y, v010.y, v110.y, v001.y, v101.y, v011.y, v111.y);
@@ -424,6 +434,88 @@ __device__ __forceinline__ T rkTrial(const FieldD &F, const T pos[3], const T di
   return (e < T(1e-20)) ? T(1e-20) : e;
 }
 
+// Mixed form: k1 = q d x B(pos) in FP64 from the paired field value, and
+// the other stages as FP32 offsets from it,
+//   k2 - k1 = q (d x (Bm - Bf) + h/2 k1 x Bm),  k3 - k1 = q (d x (Bm - Bf) + h/2 k2 x Bm),
+//   k4 - k1 = q (d x (Bl - Bf) + h k3 x Bl),
+// whose FP32 rounding is relative to the offsets (h kappa and the field's
+// change along the step times k), not to k.  The error estimate
+// k1 - k2 - k3 + k4 is a sum of offsets; the transport Jacobian takes the
+// stages' FP32 values.
+struct StagesDelta {
+  RkStages<float> s;   // FP32 stages and field values for the transport
+  double k1[3];        // k1 in FP64
+  kff::ff Bf[3];       // field at the step's start
+  float dBm[3], d2[3], d3[3], d4[3];
+};
+
+__device__ __forceinline__ void rkFirstDelta(const FieldD &F, const float posf[3], const double dir[3],
+                                             double qop, StagesDelta &S) {
+  getFieldFF(F, posf, S.Bf);
+  double B[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    B[i] = kff::join(S.Bf[i]);
+    S.s.Bf[i] = S.Bf[i].hi;
+  }
+  double c[3];
+  cross3(dir, B, c);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    S.k1[i] = qop * c[i];
+    S.s.k1[i] = (float)S.k1[i];
+  }
+}
+
+// tryRungeKuttaStep (EigenStepper.ipp:243-269) as FP32 offsets from k1; the
+// trial positions only locate the field
+__device__ __forceinline__ float rkTrialDelta(const FieldD &F, const float pos[3], const float dir[3],
+                                              float q, float h, StagesDelta &S) {
+  const float h2 = h * h, half_h = h * 0.5f;
+  float p1[3], dB[3], a[3], b[3];
+  kff::ff B[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) p1[i] = pos[i] + half_h * dir[i] + (h2 * 0.125f) * S.s.k1[i];
+  getFieldFF(F, p1, B);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    S.s.Bm[i] = B[i].hi;
+    dB[i] = (B[i].hi - S.Bf[i].hi) + (B[i].lo - S.Bf[i].lo);
+  }
+  cross3(dir, dB, a); // d x (Bm - Bf), shared by k2 and k3
+  cross3(S.s.k1, S.s.Bm, b);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    S.d2[i] = q * (a[i] + half_h * b[i]);
+    S.s.k2[i] = S.s.k1[i] + S.d2[i];
+  }
+  cross3(S.s.k2, S.s.Bm, b);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    S.d3[i] = q * (a[i] + half_h * b[i]);
+    S.s.k3[i] = S.s.k1[i] + S.d3[i];
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) p1[i] = pos[i] + h * dir[i] + (h2 * 0.5f) * S.s.k3[i];
+  getFieldFF(F, p1, B);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    S.s.Bl[i] = B[i].hi;
+    dB[i] = (B[i].hi - S.Bf[i].hi) + (B[i].lo - S.Bf[i].lo);
+  }
+  cross3(dir, dB, a);
+  cross3(S.s.k3, S.s.Bl, b);
+  float e = 0.f;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    S.d4[i] = q * (a[i] + h * b[i]);
+    S.s.k4[i] = S.s.k1[i] + S.d4[i];
+    e += fabsf(S.d4[i] - (S.d2[i] + S.d3[i])); // k1 - k2 - k3 + k4
+  }
+  e *= h2;
+  return (e < 1e-20f) ? 1e-20f : e;
+}
+
 template <typename R, typename H>
 __device__ __forceinline__ void applyTransportStep(Lane<R, H> &L, const R DA[3][3], const R DB[3][3],
                                                    const R Da[3], const R Dc[3], R D37);
@@ -611,16 +703,16 @@ template <typename R, typename H> __device__ void rkStep(Lane<R, H> &L, const Pa
 #pragma unroll
     for (int i = 0; i < 3; ++i) L.k4[i] = s.k4[i];
   } else {
-    // ---- mixed form: FP32 stages, transport and error estimate
+    // ---- mixed form: FP32 stage offsets from an FP64 k1, FP32 transport
     const float qopf = (float)L.qop;
     const float posf[3] = {(float)L.pos[0], (float)L.pos[1], (float)L.pos[2]};
     const float dirf[3] = {(float)L.dir[0], (float)L.dir[1], (float)L.dir[2]};
     const float tolLo = P.tolLoF, tolHi = P.tolHiF;
-    RkStages<float> s;
-    rkFirst<float>(P.field, posf, dirf, qopf, s);
+    StagesDelta S;
+    rkFirstDelta(P.field, posf, L.dir, L.qop, S);
     for (;;) {
       L.rkTrials++;
-      const float errf = rkTrial<float>(P.field, posf, dirf, qopf, (float)h, s);
+      const float errf = rkTrialDelta(P.field, posf, dirf, qopf, (float)h, S);
       double err = errf;
       bool accept;
       if (errf <= tolLo) {
@@ -645,16 +737,16 @@ template <typename R, typename H> __device__ void rkStep(Lane<R, H> &L, const Pa
       nTrials++;
     }
     L.t += h * L.dtds;
-    const float hf = (float)h;
-    transportUpdate<float>(L, dirf, qopf, hf, (float)L.d37, s);
-    // motion: FP64 state plus FP32 increments
-    const float hh6 = hf * hf / 6.f, h6 = hf / 6.f;
+    transportUpdate<float>(L, dirf, qopf, (float)h, (float)L.d37, S.s);
+    // motion: FP64 state, FP64 k1, FP32 sums of the offsets
+    //   pos += h d + h^2/6 (3 k1 + d2 + d3),  dir += h/6 (6 k1 + 2 (d2 + d3) + d4)
+    const double hh6 = h * h * (1. / 6.), h6 = h * (1. / 6.);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-      const float dp = hh6 * (s.k1[i] + s.k2[i] + s.k3[i]);
-      const float dd = h6 * (s.k1[i] + 2.f * (s.k2[i] + s.k3[i]) + s.k4[i]);
-      L.pos[i] = L.pos[i] + (h * L.dir[i] + (double)dp);
-      L.dir[i] = L.dir[i] + (double)dd;
+      const float s23 = S.d2[i] + S.d3[i];
+      const float s234 = 2.f * s23 + S.d4[i];
+      L.pos[i] = L.pos[i] + (h * L.dir[i] + hh6 * (3. * S.k1[i] + (double)s23));
+      L.dir[i] = L.dir[i] + h6 * (6. * S.k1[i] + (double)s234);
     }
     // |dir|^2 = 1 + e with e ~ (h kappa)^2 <= 1e-3: two Newton steps of
     // 1/sqrt from 1 reach FP64 precision (error ~ e^4)
@@ -666,7 +758,7 @@ template <typename R, typename H> __device__ void rkStep(Lane<R, H> &L, const Pa
     L.dir[1] *= f;
     L.dir[2] *= f;
 #pragma unroll
-    for (int i = 0; i < 3; ++i) L.k4[i] = s.k4[i];
+    for (int i = 0; i < 3; ++i) L.k4[i] = S.s.k4[i];
   }
   L.stepped = true;
   L.pathAcc += h;
@@ -741,9 +833,9 @@ __device__ __forceinline__ void projectCov(Lane<R, H> &L, Transported<R> &X, con
   const R cosP = x * invS, sinP = y * invS;
   const R j24 = -sinP * invS, j25 = cosP * invS;
   const R j34 = cosP * cosT, j35 = sinP * cosT, j36 = -sinT;
-  // the projection's arithmetic type: the Jacobian's (FP32 in the mixed form:
-  // covariance transport is Jacobian transport; the covariance itself stays
-  // FP64 between events, and the gain and Joseph update are FP64)
+  // the Jacobian's arithmetic type: FP32 in the mixed form (Jacobian
+  // transport); the covariance, its transport J C J^T, the gain and the
+  // Joseph update are FP64
   using CT = typename std::conditional<sizeof(R) == sizeof(float), float, double>::type;
   CT J[6][6];
 #pragma unroll
@@ -757,11 +849,20 @@ __device__ __forceinline__ void projectCov(Lane<R, H> &L, Transported<R> &X, con
   }
 #pragma unroll
   for (int r = 0; r < 6; ++r) J[r][5] = (r == 5) ? CT(1) : CT(0);
-  CT Cin[21];
+  // C' = J C J^T in FP64 in both forms.  The closed-form smoother inverts the
+  // same Jacobian, so the predicted covariance must be J C J^T to well below
+  // FP32 rounding: an FP32 product moves the fitted perigee by ~2e-6 of its
+  // resolution on the 30-plane field-map telescope.
+  double Jd[6][5];
 #pragma unroll
-  for (int e = 0; e < 21; ++e) Cin[e] = (CT)L.cov(e);
+  for (int r = 0; r < 6; ++r)
+#pragma unroll
+    for (int c = 0; c < 5; ++c) Jd[r][c] = (double)J[r][c];
+  double Cin[21];
+#pragma unroll
+  for (int e = 0; e < 21; ++e) Cin[e] = L.cov(e);
   // M = J C  (rows 0-3 and 5 use k = 0..4 (+5 for row 5), row 4 = C row 4)
-  CT M[6][6];
+  double M[6][6];
 #pragma unroll
   for (int i = 0; i < 6; ++i) {
 #pragma unroll
@@ -769,9 +870,9 @@ __device__ __forceinline__ void projectCov(Lane<R, H> &L, Transported<R> &X, con
       if (i == 4) {
         M[i][j] = Cin[sidx(4, j)];
       } else {
-        CT s = J[i][0] * Cin[sidx(0, j)];
+        double s = Jd[i][0] * Cin[sidx(0, j)];
 #pragma unroll
-        for (int k = 1; k < 5; ++k) s += J[i][k] * Cin[sidx(k, j)];
+        for (int k = 1; k < 5; ++k) s += Jd[i][k] * Cin[sidx(k, j)];
         if (i == 5) s += Cin[sidx(5, j)];
         M[i][j] = s;
       }
@@ -782,25 +883,25 @@ __device__ __forceinline__ void projectCov(Lane<R, H> &L, Transported<R> &X, con
   for (int i = 0; i < 6; ++i) {
 #pragma unroll
     for (int j = i; j < 6; ++j) {
-      CT s;
+      double s;
       if (j == 4) {
         s = M[i][4];
       } else {
-        s = M[i][0] * J[j][0];
+        s = M[i][0] * Jd[j][0];
 #pragma unroll
-        for (int k = 1; k < 5; ++k) s += M[i][k] * J[j][k];
+        for (int k = 1; k < 5; ++k) s += M[i][k] * Jd[j][k];
         if (j == 5) s += M[i][5];
       }
-      L.cov(ut(i, j)) = (double)s;
+      L.cov(ut(i, j)) = s;
     }
   }
 #pragma unroll
   for (int c = 0; c < 5; ++c) {
-    Jst[c] = J[0][c];
-    Jst[5 + c] = J[1][c];
-    Jst[10 + c] = J[2][c];
-    Jst[15 + c] = J[3][c];
-    Jst[20 + c] = J[5][c];
+    Jst[c] = Jd[0][c];
+    Jst[5 + c] = Jd[1][c];
+    Jst[10 + c] = Jd[2][c];
+    Jst[15 + c] = Jd[3][c];
+    Jst[20 + c] = Jd[5][c];
   }
 }
 
@@ -1079,9 +1180,10 @@ __device__ __forceinline__ void invJacobian(const T J[25], T Gi[25]) {
 // Smoother when no smoothed-state output is requested: only the first
 // state's covariance leaves the fit, C_s(0) = Pg C_f(n-1) Pg^T with
 // Pg = G_1 ... G_{n-1} accumulated on the Jacobian structure (~190 instead of
-// ~470 FLOP per state for G C_s' G^T).  The gains G_i = J_i^-1 and the
-// corrections G (x_s' - x_p') are formed in T (FP32 in the mixed form, FP64
-// in the plain form) and added to the FP64 filtered parameters.
+// ~470 FLOP per state for G C_s' G^T).  The gains G_i = J_i^-1 are formed in
+// T (FP32 in the mixed form, FP64 in the plain form); the corrections
+// J_i^-1 (x_s' - x_p') are FP64-accurate in both: the mixed form refines its
+// FP32 product once against the FP64 residual x_s' - x_p' - J_i y.
 template <typename T, typename R, typename H>
 __device__ bool finalizeSmoothGain(Lane<R, H> &L, const Params &P, const PlaneD *planes) {
   L.smoothed = true;
@@ -1101,25 +1203,53 @@ __device__ bool finalizeSmoothGain(Lane<R, H> &L, const Params &P, const PlaneD 
 #pragma unroll
     for (int e = 0; e < 25; ++e) nan = nan || (G[e] != G[e]);
     if (nan) return false;
-    T dx[6];
+    double dxd[6];
 #pragma unroll
-    for (int e = 0; e < 6; ++e) dx[e] = (T)(xs[e] - *wsPtr(P, L, i + 1, e));
-    T y[6];
+    for (int e = 0; e < 6; ++e) dxd[e] = xs[e] - *wsPtr(P, L, i + 1, e);
+    // y = G dx on the structure of J^-1
+    auto apply = [&](const double v[6], double out[6]) {
+      T dx[6];
 #pragma unroll
-    for (int r = 0; r < 6; ++r) {
-      if (r == 4) {
-        y[4] = dx[4];
-      } else {
-        const int gr = (r == 5) ? 4 : r;
-        T g = G[5 * gr] * dx[0];
+      for (int e = 0; e < 6; ++e) dx[e] = (T)v[e];
 #pragma unroll
-        for (int k = 1; k < 5; ++k) g += G[5 * gr + k] * dx[k];
-        if (r == 5) g += dx[5];
-        y[r] = g;
+      for (int r = 0; r < 6; ++r) {
+        if (r == 4) {
+          out[4] = (double)dx[4];
+        } else {
+          const int gr = (r == 5) ? 4 : r;
+          T g = G[5 * gr] * dx[0];
+#pragma unroll
+          for (int k = 1; k < 5; ++k) g += G[5 * gr + k] * dx[k];
+          if (r == 5) g += dx[5];
+          out[r] = (double)g;
+        }
       }
+    };
+    double y[6];
+    apply(dxd, y);
+    if constexpr (sizeof(T) == sizeof(float)) {
+      // FP32 gain: one refinement step with the residual in FP64,
+      // r = dx - J y, y += G r, makes y = J^-1 dx to FP64 accuracy
+      double rd[6], y1[6];
+#pragma unroll
+      for (int r = 0; r < 6; ++r) {
+        if (r == 4) {
+          rd[4] = dxd[4] - y[4];
+        } else {
+          const int jr = (r == 5) ? 4 : r;
+          double v = dxd[r];
+#pragma unroll
+          for (int k = 0; k < 5; ++k) v -= *wsPtr(P, L, i + 1, 12 + 5 * jr + k) * y[k];
+          if (r == 5) v -= y[5];
+          rd[r] = v;
+        }
+      }
+      apply(rd, y1);
+#pragma unroll
+      for (int e = 0; e < 6; ++e) y[e] += y1[e];
     }
 #pragma unroll
-    for (int e = 0; e < 6; ++e) xs[e] = *wsPtr(P, L, i, 6 + e) + (double)y[e];
+    for (int e = 0; e < 6; ++e) xs[e] = *wsPtr(P, L, i, 6 + e) + y[e];
     // Pg <- G Pg on the structure [[A, b, 0], [0, 1, 0], [c, d, 1]]
     T Np[25];
 #pragma unroll

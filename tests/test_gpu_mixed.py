@@ -1,6 +1,7 @@
-"""The mixed-precision form (FP32 propagation and Jacobians, FP64 Kalman
-algebra) against the FP64 oracle: same control flow on almost every track,
-small parameter errors, identical pull widths."""
+"""The mixed-precision form (FP32 field interpolation, RK stages and
+Jacobians; FP64 state, covariance transport, gain, Joseph update and smoother
+correction) against the FP64 oracle: same control flow on almost every
+track, median parameter error at most 1e-6 relative, pull widths within 1 %."""
 import numpy as np
 import pytest
 
@@ -33,8 +34,8 @@ def test_mixed_against_fp64_oracle(kf, orc, workload):
     med = np.median(rel, axis=1)
     p99 = np.percentile(rel, 99, axis=1)
     print("median", med, "p99", p99, "max", rel.max(axis=1))
-    assert np.all(med <= 1e-5), med
-    assert np.all(p99 <= 1e-4), p99
+    assert np.all(med <= 1e-6), med
+    assert np.all(p99 <= 2e-5), p99
     wg, wo = _pull_widths(g, tel, ok), _pull_widths(o, tel, ok)
     assert np.all(np.abs(wg / wo - 1) < 0.01), (wg, wo)
 
@@ -49,4 +50,4 @@ def test_mixed_holes_outliers(kf, orc):
     assert np.mean(g["status"] == o["status"]) >= 0.999
     assert np.mean(g["n_meas"] == o["n_meas"]) >= 0.999
     ok, rel = _errors(g, o)
-    assert np.all(np.median(rel, axis=1) <= 1e-5)
+    assert np.all(np.median(rel, axis=1) <= 1e-6), np.median(rel, axis=1)
