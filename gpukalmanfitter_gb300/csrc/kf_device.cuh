@@ -321,11 +321,33 @@ template <typename R, typename H> __device__ __forceinline__ void ssInit(Lane<R,
 }
 
 // per-leg constants: q/p, dt/ds and the dt/d(q/p) coefficient
-template <typename R, typename H> __device__ __forceinline__ void legConstants(Lane<R, H> &L, double mass) {
-  const double ip = 1. / L.p;
+// 1/sqrt(a), a >= 1: an FP32 estimate refined by two Newton-Raphson steps
+// y <- y (3 - a y^2) / 2 (each squares the relative error: ~1e-7 -> 1e-14 -> FP64)
+__device__ __forceinline__ double rsqrtNewton(double a) {
+  double y = (double)rsqrtf((float)a);
+  y = y * (1.5 - 0.5 * a * y * y);
+  return y * (1.5 - 0.5 * a * y * y);
+}
+
+// per-leg constants from 1/p (ip): q/p, dt/ds = sqrt(1 + (m/p)^2) and the
+// transport matrix's time-q/p factor m^2 q / (p dt/ds).  The plain form
+// follows the reference's expressions; the mixed form spends no FP64
+// division on them.
+template <typename R, typename H>
+__device__ __forceinline__ void legConstantsIp(Lane<R, H> &L, double mass, double ip) {
   L.qop = L.q * ip;
-  L.dtds = hypot(1., mass * ip);
-  L.d37 = mass * mass * L.q * ip / L.dtds;
+  if constexpr (sizeof(R) == sizeof(float)) {
+    const double x = mass * ip, a = 1. + x * x;
+    const double y = rsqrtNewton(a);
+    L.dtds = a * y;
+    L.d37 = mass * mass * L.q * ip * y;
+  } else {
+    L.dtds = hypot(1., mass * ip);
+    L.d37 = mass * mass * L.q * ip / L.dtds;
+  }
+}
+template <typename R, typename H> __device__ __forceinline__ void legConstants(Lane<R, H> &L, double mass) {
+  legConstantsIp(L, mass, 1. / L.p);
 }
 
 // ---- Jacobian resets -------------------------------------------------------
@@ -849,52 +871,70 @@ __device__ __forceinline__ void projectCov(Lane<R, H> &L, Transported<R> &X, con
   }
 #pragma unroll
   for (int r = 0; r < 6; ++r) J[r][5] = (r == 5) ? CT(1) : CT(0);
-  // C' = J C J^T in FP64 in both forms.  The closed-form smoother inverts the
-  // same Jacobian, so the predicted covariance must be J C J^T to well below
-  // FP32 rounding: an FP32 product moves the fitted perigee by ~2e-6 of its
-  // resolution on the 30-plane field-map telescope.
+  // C' = J C J^T.  The (loc, angles, q/p) block in FP64 in both forms: the
+  // closed-form smoother inverts the same Jacobian, so that block must be
+  // J C J^T to well below FP32 rounding (an FP32 product moves the fitted
+  // perigee by ~2e-6 of its resolution on the 30-plane field-map telescope).
+  // The time row and column (J(i, 5) = 0 for i < 5, so they feed nothing
+  // else) in the Jacobian's type.
   double Jd[6][5];
 #pragma unroll
   for (int r = 0; r < 6; ++r)
 #pragma unroll
     for (int c = 0; c < 5; ++c) Jd[r][c] = (double)J[r][c];
-  double Cin[21];
+  // M = J C on rows 0-3, columns 0-4 (row 4 of J is e4)
+  double M[4][5];
 #pragma unroll
-  for (int e = 0; e < 21; ++e) Cin[e] = L.cov(e);
-  // M = J C  (rows 0-3 and 5 use k = 0..4 (+5 for row 5), row 4 = C row 4)
-  double M[6][6];
+  for (int i = 0; i < 4; ++i) {
 #pragma unroll
-  for (int i = 0; i < 6; ++i) {
+    for (int j = 0; j < 5; ++j) {
+      double s = Jd[i][0] * L.cov(sidx(0, j));
 #pragma unroll
-    for (int j = 0; j < 6; ++j) {
-      if (i == 4) {
-        M[i][j] = Cin[sidx(4, j)];
-      } else {
-        double s = Jd[i][0] * Cin[sidx(0, j)];
-#pragma unroll
-        for (int k = 1; k < 5; ++k) s += Jd[i][k] * Cin[sidx(k, j)];
-        if (i == 5) s += Cin[sidx(5, j)];
-        M[i][j] = s;
-      }
+      for (int k = 1; k < 5; ++k) s += Jd[i][k] * L.cov(sidx(k, j));
+      M[i][j] = s;
     }
   }
-  // C' = M J^T (upper triangle)
+  // time: N = C J(5, :)^T with J(5, 5) = 1, C'(i, 5) = J(i, :) N
+  CT N[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    CT s = (CT)L.cov(sidx(k, 5));
+#pragma unroll
+    for (int l = 0; l < 5; ++l) s += (CT)L.cov(sidx(k, l)) * J[5][l];
+    N[k] = s;
+  }
+  CT T5[6];
 #pragma unroll
   for (int i = 0; i < 6; ++i) {
+    if (i == 4) {
+      T5[4] = N[4];
+    } else {
+      CT s = (i == 5) ? N[5] : CT(0);
 #pragma unroll
-    for (int j = i; j < 6; ++j) {
+      for (int k = 0; k < 5; ++k) s += J[i][k] * N[k];
+      T5[i] = s;
+    }
+  }
+  // C' upper triangle
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+#pragma unroll
+    for (int j = i; j < 5; ++j) {
       double s;
-      if (j == 4) {
+      if (i == 4) {
+        s = L.cov(ut(4, 4));
+      } else if (j == 4) {
         s = M[i][4];
       } else {
         s = M[i][0] * Jd[j][0];
 #pragma unroll
         for (int k = 1; k < 5; ++k) s += M[i][k] * Jd[j][k];
-        if (j == 5) s += M[i][5];
       }
       L.cov(ut(i, j)) = s;
     }
   }
+#pragma unroll
+  for (int i = 0; i < 6; ++i) L.cov(ut(i, 5)) = (double)T5[i];
 #pragma unroll
   for (int c = 0; c < 5; ++c) {
     Jst[c] = Jd[0][c];
@@ -909,6 +949,16 @@ __device__ __forceinline__ void projectCov(Lane<R, H> &L, Transported<R> &X, con
 // coordinate_transformations.hpp:115-128): angles and q/p from the momentum.
 template <typename R, typename H>
 __device__ __forceinline__ void boundAngles(const Lane<R, H> &L, double out[6], double mom[3]) {
+  if constexpr (sizeof(R) == sizeof(float)) {
+    // mixed form: |p| and q/p as the stepper holds them (no FP64 division)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) mom[i] = L.p * L.dir[i];
+    out[2] = atan2(L.dir[1], L.dir[0]);
+    out[3] = atan2(sqrt(L.dir[0] * L.dir[0] + L.dir[1] * L.dir[1]), L.dir[2]);
+    out[4] = L.qop;
+    out[5] = L.t;
+    return;
+  }
   const double qopF = L.q / L.p;
   const double pabs = fabs(1. / qopF);
   mom[0] = pabs * L.dir[0];
@@ -996,8 +1046,9 @@ __device__ __forceinline__ void stepperUpdate(Lane<R, H> &L, const PlaneD &pl, c
   sincos(par[2], &sp, &cp);
   sincos(par[3], &st, &ct);
   const double d0 = cp * st, d1 = sp * st, d2 = ct;
-  const double n = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
-  const double in = 1. / n;
+  const double n2 = d0 * d0 + d1 * d1 + d2 * d2;
+  // mixed form: |d|^2 = 1 + O(1e-16), one Newton step of 1/sqrt from 1 is exact
+  const double in = (sizeof(R) == sizeof(float)) ? 1.5 - 0.5 * n2 : 1. / sqrt(n2);
   L.dir[0] = d0 * in;
   L.dir[1] = d1 * in;
   L.dir[2] = d2 * in;
@@ -1005,7 +1056,8 @@ __device__ __forceinline__ void stepperUpdate(Lane<R, H> &L, const PlaneD &pl, c
   L.t = par[5];
 #pragma unroll
   for (int e = 0; e < 21; ++e) L.cov(e) = cov[e];
-  legConstants(L, mass);
+  if constexpr (sizeof(R) == sizeof(float)) legConstantsIp(L, mass, fabs(par[4]));
+  else legConstants(L, mass);
 }
 
 // ---------------------------------------------------------------------------
