@@ -4,7 +4,11 @@
 //
 // Objective: chi2 = sum over tracks and non-outlier measurement states of
 // (m - H x_s)^T V^-1 (m - H x_s), x_s the smoothed parameters of the fit
-// (closed-form RTS smoother).  One thread per track:
+// (closed-form RTS smoother).  One thread per track, tracks in work-queue
+// order (sorted by sequence length and curvature, kfh::sortQueue, so that a
+// warp's lanes take similar numbers of RK steps between surfaces); the
+// adjoint's own workspace is indexed by queue position (coalesced), inputs,
+// outputs and per-track gradient parts by track:
 //   A. forward fit (the fit kernel's own lane program, smoothing off) with a
 //      checkpoint of the whole lane before every 5th measurement state;
 //   B. smoother and chi2 from the stored states, then the smoother's reverse
@@ -40,13 +44,14 @@ enum { REC_STEP = 1, REC_ACT = 2, REC_HIT = 3 };
 constexpr int kStepFixed = 33;     // pos 3, dir 3, t, p, transport Jacobian 25
 
 struct AdjParams {
-  double *stateBar;  // [S][37][n] adjoints of predicted, filtered, Jacobian
-  double *xs;        // [S][6][n] smoothed parameters
-  int32_t *info;     // [S][n] plane index | outlier << 8
-  double *snap;      // [nCk][kSnapWords][n]
-  double *tape;      // [n][kTapeWords]
-  double *alignPart; // [S][6][n]
-  double *trackFs;   // [n] per-track d chi2 / d field scale
+  const int32_t *perm; // [n] queue position -> track
+  double *stateBar;  // [S][37][n] adjoints of predicted, filtered, Jacobian (by position)
+  double *xs;        // [S][6][n] smoothed parameters (by position)
+  int32_t *info;     // [S][n] plane index | outlier << 8 (by position)
+  double *snap;      // [nCk][kSnapWords][n] (by position)
+  double *tape;      // [n][kTapeWords] (by position)
+  double *alignPart; // [S][6][n] (by track)
+  double *trackFs;   // [n] per-track d chi2 / d field scale (by track)
   double *chi2;      // [n]
   int32_t *status;   // [n]
   double *gradStart; // [6][stride] or null
@@ -259,7 +264,7 @@ __device__ void runWarp(ALane &L, const Params &P, const PlaneD *sp, const AdjPa
     if (__all_sync(0xffffffffu, waiting)) {
       if (L.parked && !stopped) {
         if (ck && hitPending(L) && L.measStates > 0 && L.measStates % kEvery == 0) {
-          Saver s{A.snap + (int64_t)(L.measStates / kEvery - 1) * kSnapWords * P.n + L.idx, P.n, 0};
+          Saver s{A.snap + (int64_t)(L.measStates / kEvery - 1) * kSnapWords * P.n + L.wsIdx, P.n, 0};
           visitLane(L, s);
         }
         runEvent(L, P, sp);
@@ -390,7 +395,7 @@ __device__ void reverseAct(const double *w, const double pos[3], const double di
 // reverse of a surface event with a hit: bound state (prediction, covariance
 // transport, jacToGlobal), gain update, stepper update
 __device__ void reverseHit(const double *w, Adj &R, const Params &P, const PlaneD *sp,
-                           const AdjParams &A, int64_t i, double q) {
+                           const AdjParams &A, int64_t u, int64_t i, double q) {
   const int64_t n = P.n;
   kfa::BoundIn in;
   for (int e = 0; e < 3; ++e) {
@@ -420,10 +425,10 @@ __device__ void reverseHit(const double *w, Adj &R, const Params &P, const Plane
   kfa::BoundTmp bt;
   kfa::boundFwd(in, f, o, bt, false);
   // predicted and filtered parameters as the forward stored them
-  auto WS = [&](int e) { return P.ws[((int64_t)s * kStateStride + e) * n + i]; };
+  auto WS = [&](int e) { return P.ws[((int64_t)s * kStateStride + e) * n + u]; };
   for (int e = 0; e < 6; ++e) o.pred[e] = WS(e);
   // smoother adjoints of this state
-  const double *sb = A.stateBar + i;
+  const double *sb = A.stateBar + u;
   auto SB = [&](int e) { return sb[((int64_t)s * kStateStride + e) * n]; };
   for (int e = 0; e < 6; ++e) ob.pred[e] = SB(e);
   for (int e = 0; e < 25; ++e) ob.Jst[e] = SB(12 + e);
@@ -478,7 +483,7 @@ __device__ void reverseHit(const double *w, Adj &R, const Params &P, const Plane
 // records whenever a lane has one on top, surface events once every lane with
 // work has one on top.  Returns false for a malformed tape.
 __device__ bool reverseWarp(const double *tape, int top, Adj &R, const Params &P,
-                            const PlaneD *sp, const AdjParams &A, int64_t i, double q) {
+                            const PlaneD *sp, const AdjParams &A, int64_t u, int64_t i, double q) {
   bool bad = false;
   double cpos[3] = {0., 0., 0.}, cdir[3] = {0., 0., 0.}; // pre-state of the step after
   for (;;) {
@@ -507,7 +512,7 @@ __device__ bool reverseWarp(const double *tape, int top, Adj &R, const Params &P
     } else {
       if (!__any_sync(0xffffffffu, type == REC_HIT)) break;
       if (type == REC_HIT) {
-        reverseHit(tape + (top - len), R, P, sp, A, i, q);
+        reverseHit(tape + (top - len), R, P, sp, A, u, i, q);
         top -= len;
       }
     }
@@ -517,11 +522,12 @@ __device__ bool reverseWarp(const double *tape, int top, Adj &R, const Params &P
 
 // smoothed chi2 of one track from its stored states; with grad, the adjoints
 // of every state's predicted and filtered parameters and Jacobian
-__device__ double smoothChi2(const Params &P, const AdjParams &A, int64_t i, int ns, bool grad) {
+__device__ double smoothChi2(const Params &P, const AdjParams &A, int64_t u, int64_t i, int ns,
+                             bool grad) {
   const int64_t n = P.n;
-  auto WS = [&](int s, int e) { return P.ws[((int64_t)s * kStateStride + e) * n + i]; };
-  auto XS = [&](int s, int e) -> double & { return A.xs[((int64_t)s * 6 + e) * n + i]; };
-  auto SB = [&](int s, int e) -> double & { return A.stateBar[((int64_t)s * kStateStride + e) * n + i]; };
+  auto WS = [&](int s, int e) { return P.ws[((int64_t)s * kStateStride + e) * n + u]; };
+  auto XS = [&](int s, int e) -> double & { return A.xs[((int64_t)s * 6 + e) * n + u]; };
+  auto SB = [&](int s, int e) -> double & { return A.stateBar[((int64_t)s * kStateStride + e) * n + u]; };
   double xs[6];
   for (int e = 0; e < 6; ++e) xs[e] = WS(ns - 1, 6 + e);
   for (int e = 0; e < 6; ++e) XS(ns - 1, e) = xs[e];
@@ -541,7 +547,7 @@ __device__ double smoothChi2(const Params &P, const AdjParams &A, int64_t i, int
   double chi2 = 0.;
   auto term = [&](int s, double g[2]) {
     g[0] = g[1] = 0.;
-    const int inf = A.info[(int64_t)s * n + i];
+    const int inf = A.info[(int64_t)s * n + u];
     if (inf & 256) return;
     const int k = inf & 255;
     const double *mp = P.meas + (size_t)k * 5 * P.stride + i;
@@ -610,24 +616,25 @@ __global__ void __launch_bounds__(kLaneSlots, KF_ADJ_MIN_BLOCKS)
   __syncthreads();
   // every lane stays to the end: the lane program and the reverse sweep run
   // warp-synchronously (idle lanes carry no work)
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool valid = i < P.n;
+  const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; // queue position
+  const bool valid = u < P.n;
+  const int64_t i = valid ? (int64_t)A.perm[u] : 0;                 // track
   ALane L;
-  L.hook.tape = A.tape + (valid ? i : 0) * kTapeWords;
-  L.hook.info = A.info + (valid ? i : 0);
+  L.hook.tape = A.tape + (valid ? u : 0) * kTapeWords;
+  L.hook.info = A.info + (valid ? u : 0);
   L.hook.n = P.n;
   L.hook.top = L.hook.head = L.hook.state = L.hook.plane = 0;
   L.hook.rec = false;
   L.hook.full = false;
   if (valid) zeroTrack(P, A, i);
   // ---- A: forward fit with checkpoints
-  initLane(L, P, sp, valid ? i : -1, valid ? i : 0);
+  initLane(L, P, sp, valid ? i : -1, valid ? u : 0);
   runWarp(L, P, sp, A, -1, A.grad != 0);
   const int ns = L.measStates;
   const bool ok = valid && L.status == KF_TRACK_OK && ns > 0;
   if (valid) A.status[i] = L.status;
   // ---- B: smoothed chi2 (and the smoother's adjoints)
-  if (ok) A.chi2[i] = smoothChi2(P, A, i, ns, A.grad != 0);
+  if (ok) A.chi2[i] = smoothChi2(P, A, u, i, ns, A.grad != 0);
   if (!A.grad) return;
   // ---- C: segments, last first, all lanes together
   Adj R;
@@ -644,15 +651,15 @@ __global__ void __launch_bounds__(kLaneSlots, KF_ADJ_MIN_BLOCKS)
       L.pc = PC_DONE;
       L.parked = false;
     } else if (c == 0) {
-      initLane(L, P, sp, i, i);
+      initLane(L, P, sp, i, u);
     } else {
-      Loader ld{A.snap + (int64_t)(c - 1) * kSnapWords * P.n + i, P.n, 0};
+      Loader ld{A.snap + (int64_t)(c - 1) * kSnapWords * P.n + u, P.n, 0};
       visitLane(L, ld);
     }
     runWarp(L, P, sp, A, (c + 1) * kEvery, false);
     if (act && L.hook.full) failed = true;
     const bool sweep = act && !failed;
-    if (!reverseWarp(L.hook.tape, sweep ? L.hook.top : 0, R, P, sp, A, i, q) && sweep)
+    if (!reverseWarp(L.hook.tape, sweep ? L.hook.top : 0, R, P, sp, A, u, i, q) && sweep)
       failed = true;
   }
   if (!ok) return;
@@ -698,7 +705,7 @@ __global__ void __launch_bounds__(256) reduceTracks(const double *src, int64_t n
 size_t alignUp(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct AdjLayout {
-  size_t ws, stateBar, xs, info, snap, tape, alignPart, trackFs, total;
+  size_t ws, stateBar, xs, info, snap, tape, alignPart, trackFs, perm, hist, offs, total;
 };
 AdjLayout adjLayout(int64_t n, int32_t S) {
   AdjLayout L{};
@@ -717,6 +724,9 @@ AdjLayout adjLayout(int64_t n, int32_t S) {
   L.tape = take((size_t)kTapeWords * n * 8);
   L.alignPart = take((size_t)S * 6 * n * 8);
   L.trackFs = take((size_t)n * 8);
+  L.perm = take((size_t)n * 4);
+  L.hist = take((size_t)kSortBuckets * 4);
+  L.offs = take((size_t)kSortBuckets * 4);
   L.total = o;
   return L;
 }
@@ -773,6 +783,7 @@ int32_t kf_adjoint_batch(const kf_inputs_t *in, kf_adjoint_outputs_t *out, const
   fillParams(P, in, &none, &c, geo, field, base + L.ws);
   AdjParams A;
   std::memset(&A, 0, sizeof(A));
+  A.perm = reinterpret_cast<const int32_t *>(base + L.perm);
   A.stateBar = reinterpret_cast<double *>(base + L.stateBar);
   A.xs = reinterpret_cast<double *>(base + L.xs);
   A.info = reinterpret_cast<int32_t *>(base + L.info);
@@ -787,6 +798,10 @@ int32_t kf_adjoint_batch(const kf_inputs_t *in, kf_adjoint_outputs_t *out, const
   A.gradStart = compute_gradient ? out->grad_start : nullptr;
   for (int a = 0; a < 3; ++a) A.B0[a] = field->value[a];
   A.grad = compute_gradient != 0;
+  rc = sortQueue(P, reinterpret_cast<int32_t *>(base + L.hist),
+                 reinterpret_cast<int32_t *>(base + L.offs),
+                 reinterpret_cast<int32_t *>(base + L.perm), s);
+  if (rc) return rc;
   const unsigned grid = (unsigned)((n + kLaneSlots - 1) / kLaneSlots);
   adjointKernel<<<grid, kLaneSlots, coldStateBytes<double>(), s>>>(P, A);
   cudaError_t e = cudaGetLastError();

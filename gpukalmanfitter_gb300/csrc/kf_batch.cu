@@ -93,7 +93,7 @@ const Variant *findVariant(const kf_config_t *cfg) {
   return nullptr;
 }
 
-constexpr int kBuckets = 2048;
+constexpr int kBuckets = kSortBuckets;
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
@@ -157,21 +157,32 @@ __global__ void scatterPerm(const __grid_constant__ Params P, int32_t *offs, int
   if (i < P.n) perm[atomicAdd(&offs[workKey(P, i)], 1)] = (int32_t)i;
 }
 
-int32_t enqueueBatched(const Params &P, const Variant *v, char *base, const BatchLayout &L,
+} // namespace
+
+int32_t kfh::sortQueue(const Params &P, int32_t *hist, int32_t *offs, int32_t *perm,
                        cudaStream_t s) {
   if (P.n == 0) return KF_SUCCESS;
-  int32_t *hist = reinterpret_cast<int32_t *>(base + L.hist);
-  int32_t *offs = reinterpret_cast<int32_t *>(base + L.offs);
-  int32_t *perm = reinterpret_cast<int32_t *>(base + L.perm);
   cudaError_t e = cudaMemsetAsync(hist, 0, kBuckets * sizeof(int32_t), s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(base + L.counter, 0, sizeof(int32_t), s);
-  if (e != cudaSuccess) return cudaFail(e, "batched queue reset");
+  if (e != cudaSuccess) return cudaFail(e, "work-queue reset");
   const unsigned g = (unsigned)((P.n + 255) / 256);
   keyHistogram<<<g, 256, 0, s>>>(P, hist);
   scanOffsets<<<1, 1024, 0, s>>>(hist, offs);
   scatterPerm<<<g, 256, 0, s>>>(P, offs, perm);
   e = cudaGetLastError();
-  if (e != cudaSuccess) return cudaFail(e, "work-queue sort");
+  return e == cudaSuccess ? KF_SUCCESS : cudaFail(e, "work-queue sort");
+}
+
+namespace {
+
+int32_t enqueueBatched(const Params &P, const Variant *v, char *base, const BatchLayout &L,
+                       cudaStream_t s) {
+  if (P.n == 0) return KF_SUCCESS;
+  cudaError_t e = cudaMemsetAsync(base + L.counter, 0, sizeof(int32_t), s);
+  if (e != cudaSuccess) return cudaFail(e, "batched queue reset");
+  const int32_t rc = sortQueue(P, reinterpret_cast<int32_t *>(base + L.hist),
+                               reinterpret_cast<int32_t *>(base + L.offs),
+                               reinterpret_cast<int32_t *>(base + L.perm), s);
+  if (rc) return rc;
   e = v->launch(P, s);
   if (e != cudaSuccess) return cudaFail(e, "persistent fit launch");
   return KF_SUCCESS;

@@ -16,6 +16,11 @@ size_t wsBytes(int64_t n, int32_t nSurf);
 // argument checks shared by every fit entry point
 int32_t checkCommon(const kf_inputs_t *in, const kf_config_t *cfg, const kf_geometry_t *geo,
                     const kf_field_t *field);
+// work-queue order of P.n tracks (kf_batch.cu): perm[position] = track, longest
+// and most curved first; hist and offs hold kSortBuckets ints each
+constexpr int kSortBuckets = 2048;
+int32_t sortQueue(const kfd::Params &P, int32_t *hist, int32_t *offs, int32_t *perm,
+                  cudaStream_t s);
 // kernel parameter block from the ABI structures
 void fillParams(kfd::Params &P, const kf_inputs_t *in, const kf_outputs_t *out,
                 const kf_config_t *cfg, const kf_geometry_t *geo, const kf_field_t *field,
