@@ -880,16 +880,28 @@ KF_HD void boundFwd(const BoundIn &in, const Frame &f, BoundOut &o, BoundTmp &w,
     J[5][c] = w.R3[c];
   }
   for (int r = 0; r < 6; ++r) J[r][5] = (r == 5) ? 1. : 0.;
+  // M = J C and C' = M J^T on the structure: row 4 of J is e4, column 5 is e5
   for (int i = 0; i < 6; ++i)
     for (int j = 0; j < 6; ++j) {
+      if (i == 4) {
+        w.M[4][j] = in.C[si6(4, j)];
+        continue;
+      }
       double s = 0.;
-      for (int k = 0; k < 6; ++k) s += J[i][k] * in.C[si6(k, j)];
+      for (int k = 0; k < 5; ++k) s += J[i][k] * in.C[si6(k, j)];
+      if (i == 5) s += in.C[si6(5, j)];
       w.M[i][j] = s;
     }
   for (int i = 0; i < (full ? 6 : 2); ++i)
     for (int j = i; j < 6; ++j) {
-      double s = 0.;
-      for (int k = 0; k < 6; ++k) s += w.M[i][k] * J[j][k];
+      double s;
+      if (j == 4) {
+        s = w.M[i][4];
+      } else {
+        s = 0.;
+        for (int k = 0; k < 5; ++k) s += w.M[i][k] * J[j][k];
+        if (j == 5) s += w.M[i][5];
+      }
       o.Cp[ut6(i, j)] = s;
     }
   for (int c = 0; c < 5; ++c) {
@@ -980,11 +992,12 @@ KF_HD void boundVjp(const BoundIn &in, const Frame &f, const BoundOut &o, const 
     kb.g46[r][0] = ob.G.g46[r][0];
     kb.g46[r][1] = ob.G.g46[r][1];
   }
-  // ---- C' = J C J^T and the stored Jacobian
-  double W[6][6], Jb[6][6];
+  // ---- C' = J C J^T and the stored Jacobian (J: row 4 = e4, column 5 = e5;
+  // W: the upper-triangle adjoint of C')
+  double Ws[6][6], Jb[6][6];
   for (int i = 0; i < 6; ++i)
     for (int j = 0; j < 6; ++j) {
-      W[i][j] = (i <= j) ? ob.Cp[ut6(i, j)] : 0.;
+      Ws[i][j] = (i == j) ? 2. * ob.Cp[ut6(i, i)] : ob.Cp[ut6(i < j ? i : j, i < j ? j : i)];
       Jb[i][j] = 0.;
     }
   const double(&J)[6][6] = w.Jf;
@@ -993,22 +1006,37 @@ KF_HD void boundVjp(const BoundIn &in, const Frame &f, const BoundOut &o, const 
     if (a == 4) continue;
     for (int b = 0; b < 5; ++b) {
       double s = 0.;
-      for (int i = 0; i < 6; ++i) s += (W[a][i] + W[i][a]) * w.M[i][b];
+      for (int i = 0; i < 6; ++i) s += Ws[a][i] * w.M[i][b];
       Jb[a][b] += s;
     }
   }
-  // C-bar (full) = J^T (W J), folded onto the stored upper triangle
+  // C-bar (full) = J^T (W J), folded onto the stored upper triangle; W is upper
+  // triangular, so row i of W J sums over j >= i
   double WJ[6][6];
   for (int i = 0; i < 6; ++i)
     for (int l = 0; l < 6; ++l) {
-      double t = 0.;
-      for (int j = 0; j < 6; ++j) t += W[i][j] * J[j][l];
+      double t;
+      if (l == 5) {
+        t = ob.Cp[ut6(i, 5)];
+      } else {
+        t = 0.;
+        for (int j = i; j < 6; ++j)
+          if (j != 4) t += ob.Cp[ut6(i, j)] * J[j][l];
+        if (l == 4 && i <= 4) t += ob.Cp[ut6(i, 4)];
+      }
       WJ[i][l] = t;
     }
   for (int k = 0; k < 6; ++k)
     for (int l = 0; l < 6; ++l) {
-      double s = 0.;
-      for (int i = 0; i < 6; ++i) s += J[i][k] * WJ[i][l];
+      double s;
+      if (k == 5) {
+        s = WJ[5][l];
+      } else {
+        s = 0.;
+        for (int i = 0; i < 6; ++i)
+          if (i != 4) s += J[i][k] * WJ[i][l];
+        if (k == 4) s += WJ[4][l];
+      }
       ib.C[si6(k, l)] += s;
     }
   for (int c = 0; c < 5; ++c) {
