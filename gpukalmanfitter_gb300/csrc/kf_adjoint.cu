@@ -244,6 +244,11 @@ template <class V> __device__ void visitLane(ALane &L, V &v) {
     }
 }
 
+// first measurement state of a lane's last checkpoint segment
+__device__ __forceinline__ int lastSegmentStart(const ALane &L) {
+  return L.nHits > 0 ? (L.nHits - 1) / kEvery * kEvery : 0;
+}
+
 __device__ __forceinline__ bool hitPending(const ALane &L) {
   return L.parked && L.current >= 0 && !L.smoothed && !L.finished &&
          ((L.mask >> L.current) & 1ull);
@@ -252,8 +257,10 @@ __device__ __forceinline__ bool hitPending(const ALane &L) {
 // Run the lane program of every lane of the warp (all 32 lanes call it) until
 // each is done or parked before the hit event of measurement state stopAt
 // (stopAt < 0: never).  As in the fit kernel, lanes step independently and
-// run their surface events together once every lane waits.  With ck, a lane
-// saves itself before the hit events of states 5, 10, ...
+// run their surface events together once every lane waits.  With ck (the
+// forward of a gradient run), a lane saves itself before the hit events of
+// states 5, 10, ... and records the tape of its last segment as it runs it:
+// the reverse sweep starts there without recomputing it.
 __device__ void runWarp(ALane &L, const Params &P, const PlaneD *sp, const AdjParams &A,
                         int stopAt, bool ck) {
   bool stopped = false;
@@ -266,6 +273,10 @@ __device__ void runWarp(ALane &L, const Params &P, const PlaneD *sp, const AdjPa
         if (ck && hitPending(L) && L.measStates > 0 && L.measStates % kEvery == 0) {
           Saver s{A.snap + (int64_t)(L.measStates / kEvery - 1) * kSnapWords * P.n + L.wsIdx, P.n, 0};
           visitLane(L, s);
+          if (L.measStates == lastSegmentStart(L)) {
+            L.hook.top = 0;
+            L.hook.rec = true;
+          }
         }
         runEvent(L, P, sp);
       }
@@ -627,8 +638,9 @@ __global__ void __launch_bounds__(kLaneSlots, KF_ADJ_MIN_BLOCKS)
   L.hook.rec = false;
   L.hook.full = false;
   if (valid) zeroTrack(P, A, i);
-  // ---- A: forward fit with checkpoints
+  // ---- A: forward fit with checkpoints (and the last segment's tape)
   initLane(L, P, sp, valid ? i : -1, valid ? u : 0);
+  L.hook.rec = valid && A.grad != 0 && lastSegmentStart(L) == 0;
   runWarp(L, P, sp, A, -1, A.grad != 0);
   const int ns = L.measStates;
   const bool ok = valid && L.status == KF_TRACK_OK && ns > 0;
@@ -645,9 +657,10 @@ __global__ void __launch_bounds__(kLaneSlots, KF_ADJ_MIN_BLOCKS)
   bool failed = false;
   for (int c = maxSeg - 1; c >= 0; --c) {
     const bool act = ok && !failed && c < nseg;
-    L.hook.top = 0;
-    L.hook.rec = act;
-    if (!act) {
+    const bool taped = act && c == nseg - 1; // recorded by the forward
+    if (!taped) L.hook.top = 0;
+    L.hook.rec = act && !taped;
+    if (!act || taped) {
       L.pc = PC_DONE;
       L.parked = false;
     } else if (c == 0) {
