@@ -386,14 +386,15 @@ def run_gpu(args) -> None:
     suite = None
     wanted = [] if args.no_suite else [x for x in args.suite.split(",") if x and x != "none"]
     if wanted and world == 1:
-        # uneven tracks (4x the headline batch), the field map (1x), the adjoint (1/4)
+        # uneven tracks (4x the headline batch), the field map (1x), the adjoint
+        # (262144 tracks at the default 1M, the differentiation workload's size)
         makers = {
             "batching": lambda: suite_entry(kf, "holes30", 4 * n, 1234567892, stream, barrier, 3, 3,
                                             [("batched_fp64", "fp64"), ("batched_mixed", "mixed")]),
             "precision_map": lambda: suite_entry(kf, "map30", n, 1234567893, stream, barrier, 3, 3,
                                                  [("batched_mixed", "mixed"), ("batched_fp64", "fp64")]),
-            "differentiation": lambda: adjoint_entry(kf, max(1, n // 4), 1234567894, stream,
-                                                     barrier, 3, 3),
+            "differentiation": lambda: adjoint_entry(kf, max(1, n * 262144 // 1000000),
+                                                     1234567894, stream, barrier, 3, 3),
         }
         suite = {k: makers[k]() for k in makers if k in wanted}
 

@@ -339,15 +339,19 @@ __device__ __forceinline__ void routeStep(Adj &R, int idx, double hb) {
 
 // reverse of one RK step record (the uniform-field step of the fit,
 // kfa::polyAcceptFwd, and the error estimates of its rejected trials)
-__device__ void reverseStep(const double *w, int len, Adj &R, const Params &P, double q) {
+// g / gp: the leg constants of momentum gp, kept across the steps of a leg
+__device__ void reverseStep(const double *w, int len, Adj &R, const Params &P, double q,
+                            kfa::Leg &g, double &gp) {
   const double *pos = w, *dir = w + 3;
   const double t = w[6], p = w[7];
   kfa::JT J0;
   readJT(w + 8, J0);
   const int T = (len - kStepFixed - 1) / 2;
   const double *tr = w + kStepFixed;
-  kfa::Leg g;
-  kfa::legFwd(p, q, P.mass, g);
+  if (p != gp) {
+    kfa::legFwd(p, q, P.mass, g);
+    gp = p;
+  }
   const double *B = P.field.B;
   const double h = tr[2 * (T - 1)];
   kfa::PolyStep ps;
@@ -497,6 +501,8 @@ __device__ bool reverseWarp(const double *tape, int top, Adj &R, const Params &P
                             const PlaneD *sp, const AdjParams &A, int64_t u, int64_t i, double q) {
   bool bad = false;
   double cpos[3] = {0., 0., 0.}, cdir[3] = {0., 0., 0.}; // pre-state of the step after
+  kfa::Leg leg;
+  double legP = -1.;
   for (;;) {
     int type = 0, len = 0;
     if (top > 0 && !bad) {
@@ -511,7 +517,7 @@ __device__ bool reverseWarp(const double *tape, int top, Adj &R, const Params &P
     if (__any_sync(0xffffffffu, type == REC_STEP || type == REC_ACT)) {
       if (type == REC_STEP) {
         const double *w = tape + (top - len);
-        reverseStep(w, len, R, P, q);
+        reverseStep(w, len, R, P, q, leg, legP);
         for (int e = 0; e < 3; ++e) {
           cpos[e] = w[e];
           cdir[e] = w[3 + e];
