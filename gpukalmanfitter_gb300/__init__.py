@@ -44,12 +44,14 @@ class KfConfig(C.Structure):
                 ("mass", C.c_double), ("overstep_limit", C.c_double),
                 ("on_surface_tol", C.c_double), ("outlier_chi2_cut", C.c_double),
                 ("faithful_jacobian", C.c_int32), ("kernel", C.c_int32),
-                ("block_size", C.c_int32), ("min_blocks_per_sm", C.c_int32)]
+                ("block_size", C.c_int32), ("min_blocks_per_sm", C.c_int32),
+                ("material_effects", C.c_int32), ("reserved0", C.c_int32)]
 
 
 class KfGeometry(C.Structure):
     _fields_ = [("n_planes", C.c_int32), ("reserved0", C.c_int32),
-                ("center", C.POINTER(C.c_double)), ("rotation", C.POINTER(C.c_double))]
+                ("center", C.POINTER(C.c_double)), ("rotation", C.POINTER(C.c_double)),
+                ("material", C.POINTER(C.c_double))]
 
 
 class KfField(C.Structure):
@@ -82,7 +84,8 @@ class SynthConfig(C.Structure):
                 ("outlier_shift", C.c_double), ("seed_loc_sigma", C.c_double),
                 ("seed_angle_sigma", C.c_double), ("seed_qop_rel", C.c_double),
                 ("seed_time_sigma", C.c_double), ("mis_shift_sigma", C.c_double),
-                ("mis_rot_sigma", C.c_double), ("rk_step", C.c_double)]
+                ("mis_rot_sigma", C.c_double), ("rk_step", C.c_double),
+                ("material", C.c_double * 6)]
 
 
 _LIB = None
@@ -190,12 +193,14 @@ class Telescope:
     truth_center: np.ndarray | None = None
     truth_rotation: np.ndarray | None = None
     misalignment: np.ndarray | None = None  # [S,6]
+    material: np.ndarray | None = None      # [S,6] surface material (None: vacuum)
 
     def geometry(self) -> tuple[KfGeometry, tuple]:
         c = np.ascontiguousarray(self.center, dtype=np.float64)
         r = np.ascontiguousarray(self.rotation, dtype=np.float64)
-        g = KfGeometry(self.n_surfaces, 0, _ptr(c), _ptr(r))
-        return g, (c, r)
+        m = None if self.material is None else np.ascontiguousarray(self.material, dtype=np.float64)
+        g = KfGeometry(self.n_surfaces, 0, _ptr(c), _ptr(r), _ptr(m) if m is not None else None)
+        return g, (c, r, m)
 
     def field(self, grid_ptr: int | None = None, scale: float = 1.0) -> KfField:
         f = KfField()
@@ -213,6 +218,13 @@ class Telescope:
         return f
 
 
+def silicon(thickness_mm: float) -> np.ndarray:
+    """Surface material row (thickness, X0, L0, Ar, Z, molar density) of
+    silicon, as the reference's test helper builds it (Test/Helper.hpp:25-29:
+    X0 9.370 cm, L0 46.52 cm, Ar 28.0855, Z 14, 2.329 g/cm^3)."""
+    return np.array([thickness_mm, 93.70, 465.2, 28.0855, 14.0, (2.329 / 28.0855) / 1000.0])
+
+
 def synth_config(**kw) -> SynthConfig:
     c = SynthConfig()
     load().kf_synth_config_default(C.byref(c))
@@ -226,13 +238,20 @@ def make_telescope(n: int, *, seed: int = 1234567890, n_planes: int = 10,
                    max_len: int | None = None, hit_prob: float = 1.0,
                    outlier_prob: float = 0.0, field_map: bool = False, field_n: int = 101,
                    field_half: float = 1500.0, mis_shift: float = 0.0, mis_rot: float = 0.0,
-                   threads: int = 0, **extra) -> Telescope:
-    """Seeded synthetic telescope workload (host arrays)."""
+                   material: float = 0.0, threads: int = 0, **extra) -> Telescope:
+    """Seeded synthetic telescope workload (host arrays).  material > 0: every
+    plane carries that many mm of silicon (the reference driver's 0.5 mm,
+    Run/GPU/KalmanFitterGPUTest.cu:253) in the geometry and in the truth."""
     lib = load()
     cfg = synth_config(n_tracks=n, seed=seed, n_planes=n_planes, x_first=x_first, x_step=x_step,
                        min_len=min_len or n_planes, max_len=max_len or n_planes,
                        hit_prob=hit_prob, outlier_prob=outlier_prob,
                        mis_shift_sigma=mis_shift, mis_rot_sigma=mis_rot, **extra)
+    mat = None
+    if material > 0:
+        mat = np.tile(silicon(material), (n_planes, 1))
+        for e in range(6):
+            cfg.material[e] = mat[0, e]
     S = n_planes
     center = np.zeros((S, 3)); rot = np.zeros((S, 9))
     tcenter = np.zeros((S, 3)); trot = np.zeros((S, 9)); align = np.zeros((S, 6))
@@ -249,7 +268,7 @@ def make_telescope(n: int, *, seed: int = 1234567890, n_planes: int = 10,
     per = np.zeros((3, n)); truth = np.zeros((6, n))
     tel = Telescope(n, S, center, rot, meas, mask, nplanes, start, scov, per, truth,
                     cfg.bz_tesla, grid, field_n if field_map else 0, field_half,
-                    tcenter, trot, align)
+                    tcenter, trot, align, mat)
     if field_map:
         field = tel.field()
     _check(lib.kf_synth_tracks(C.byref(cfg), _ptr(tcenter), _ptr(trot),
@@ -516,7 +535,8 @@ class AdjointBatch:
             c, r = align_geometry(self.center, self.rotation, np.asarray(alignment, np.float64))
         c = np.ascontiguousarray(c, dtype=np.float64)
         r = np.ascontiguousarray(r, dtype=np.float64)
-        geo = KfGeometry(self.tel.n_surfaces, 0, _ptr(c), _ptr(r))
+        m = None if self.tel.material is None else np.ascontiguousarray(self.tel.material, np.float64)
+        geo = KfGeometry(self.tel.n_surfaces, 0, _ptr(c), _ptr(r), _ptr(m) if m is not None else None)
         field = self.tel.field(scale=field_scale)
         _check(load().kf_adjoint_batch(C.byref(self.ins), C.byref(self.aout), C.byref(self.cfg),
                                        C.byref(geo), C.byref(field), C.c_int32(1 if grad else 0),

@@ -735,7 +735,7 @@ AdjLayout adjLayout(int64_t n, int32_t S) {
     return at;
   };
   const int nCk = (S - 1) / kEvery; // checkpoints before states 5, 10, ... < S
-  L.ws = take(wsBytes(n, S));
+  L.ws = take(wsBytes(n, S, false));
   L.stateBar = take((size_t)S * kStateStride * n * 8);
   L.xs = take((size_t)S * 6 * n * 8);
   L.info = take((size_t)S * n * 4);
@@ -778,6 +778,8 @@ int32_t kf_adjoint_batch(const kf_inputs_t *in, kf_adjoint_outputs_t *out, const
     return fail(KF_ERR_UNSUPPORTED, "the adjoint supports a uniform field only%s");
   if (!cfg->faithful_jacobian)
     return fail(KF_ERR_UNSUPPORTED, "the adjoint follows faithful_jacobian = 1 only%s");
+  if (cfg->material_effects && geo->material)
+    return fail(KF_ERR_UNSUPPORTED, "the adjoint has no material effects%s");
   const int64_t n = in->n_tracks;
   const int32_t S = in->n_surfaces;
   cudaStream_t s = static_cast<cudaStream_t>(stream);

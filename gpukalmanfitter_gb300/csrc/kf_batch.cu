@@ -100,7 +100,7 @@ size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 struct BatchLayout {
   size_t ws, perm, hist, offs, counter, total;
 };
-BatchLayout batchLayout(int64_t n, int32_t S) {
+BatchLayout batchLayout(int64_t n, int32_t S, bool material) {
   BatchLayout L{};
   size_t o = 0;
   auto take = [&](size_t bytes) {
@@ -108,7 +108,7 @@ BatchLayout batchLayout(int64_t n, int32_t S) {
     o = align256(o + bytes);
     return at;
   };
-  L.ws = take(wsBytes(n, S));
+  L.ws = take(wsBytes(n, S, material));
   L.perm = take((size_t)n * sizeof(int32_t));
   L.hist = take(kBuckets * sizeof(int32_t));
   L.offs = take(kBuckets * sizeof(int32_t));
@@ -205,7 +205,7 @@ int32_t prepare(const kf_inputs_t *in, kf_outputs_t *out, const kf_config_t *cfg
     const cudaError_t e = v->prep();
     if (e != cudaSuccess) return cudaFail(e, "persistent kernel shared-memory set-up");
   }
-  L = batchLayout(in->n_tracks, in->n_surfaces);
+  L = batchLayout(in->n_tracks, in->n_surfaces, cfg->material_effects != 0);
   if (in->n_tracks > 0 && (!workspace || bytes < L.total))
     return fail(KF_ERR_WORKSPACE_TOO_SMALL, "workspace smaller than kf_batch_workspace_size()%s");
   char *base = static_cast<char *>(workspace);
@@ -227,7 +227,7 @@ extern "C" {
 size_t kf_batch_workspace_size(const kf_config_t *cfg, int64_t n_tracks, int32_t n_surfaces) {
   (void)cfg;
   if (n_tracks <= 0 || n_surfaces <= 0) return 0;
-  return batchLayout(n_tracks, n_surfaces).total;
+  return batchLayout(n_tracks, n_surfaces, cfg && cfg->material_effects).total;
 }
 
 int32_t kf_fit_batch_sorted(const kf_inputs_t *in, kf_outputs_t *out, const kf_config_t *cfg,

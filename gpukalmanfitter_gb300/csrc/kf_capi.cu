@@ -40,8 +40,10 @@ int32_t cudaFail(cudaError_t e, const char *where) {
   return KF_ERR_CUDA;
 }
 
-size_t wsBytes(int64_t n, int32_t nSurf) {
-  return (size_t)nSurf * kStateStride * (size_t)n * sizeof(double);
+size_t wsBytes(int64_t n, int32_t nSurf, bool material) {
+  // per state: predicted and filtered parameters and the Jacobian; with
+  // material also the predicted and filtered covariance (general smoother)
+  return (size_t)nSurf * (kStateStride + (material ? 42 : 0)) * (size_t)n * sizeof(double);
 }
 
 int32_t checkCommon(const kf_inputs_t *in, const kf_config_t *cfg, const kf_geometry_t *geo,
@@ -132,7 +134,12 @@ void fillParams(Params &P, const kf_inputs_t *in, const kf_outputs_t *out, const
       pl.V[r] = geo->rotation[9 * k + 3 * r + 1];
       pl.T[r] = geo->rotation[9 * k + 3 * r + 2];
     }
+    for (int e = 0; e < 6; ++e) pl.mat[e] = geo->material ? geo->material[6 * k + e] : 0.;
   }
+  P.materialEffects = (geo->material && cfg->material_effects) ? (cfg->material_effects & 3) : 0;
+  P.wsCov = cfg->material_effects
+                ? static_cast<double *>(ws) + (size_t)in->n_surfaces * kStateStride * (size_t)P.wsStride
+                : nullptr;
 }
 
 } // namespace kfh
@@ -181,7 +188,7 @@ void kf_config_default(kf_config_t *c) {
 size_t kf_workspace_size(const kf_config_t *cfg, int64_t n_tracks, int32_t n_surfaces) {
   (void)cfg;
   if (n_tracks <= 0 || n_surfaces <= 0) return 0;
-  return wsBytes(n_tracks, n_surfaces);
+  return wsBytes(n_tracks, n_surfaces, cfg && cfg->material_effects);
 }
 
 int32_t kf_fit_batch(const kf_inputs_t *in, kf_outputs_t *out, const kf_config_t *cfg,
@@ -193,7 +200,8 @@ int32_t kf_fit_batch(const kf_inputs_t *in, kf_outputs_t *out, const kf_config_t
     return fail(KF_ERR_INVALID_ARGUMENT, "missing output array%s");
   if (in->n_tracks > 0 && (!in->meas || !in->start_params || !in->start_cov || !in->perigee))
     return fail(KF_ERR_INVALID_ARGUMENT, "missing input array%s");
-  if (workspace_bytes < wsBytes(in->n_tracks, in->n_surfaces) || (!workspace && in->n_tracks > 0))
+  if (workspace_bytes < wsBytes(in->n_tracks, in->n_surfaces, cfg->material_effects != 0) ||
+      (!workspace && in->n_tracks > 0))
     return fail(KF_ERR_WORKSPACE_TOO_SMALL, "workspace smaller than kf_workspace_size()%s");
   Params P;
   fillParams(P, in, out, cfg, geo, field, workspace);
@@ -207,7 +215,7 @@ struct Staging {
   size_t params, cov, chi2, status, nmeas, nsteps, ntrials, smoothed, ws, total;
 };
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
-Staging stagingLayout(int64_t n, int32_t S, bool withSmoothed) {
+Staging stagingLayout(int64_t n, int32_t S, bool withSmoothed, const kf_config_t *cfg) {
   Staging L{};
   size_t o = 0;
   auto take = [&](size_t bytes) {
@@ -230,7 +238,8 @@ Staging stagingLayout(int64_t n, int32_t S, bool withSmoothed) {
   L.ntrials = take((size_t)n * 4);
   L.smoothed = withSmoothed ? take((size_t)S * 27 * n * 8) : 0;
   // room for either form's workspace (the batched form adds its queue)
-  L.ws = take(std::max(wsBytes(n, S), kf_batch_workspace_size(nullptr, n, S)));
+  const bool mat = cfg && cfg->material_effects;
+  L.ws = take(std::max(wsBytes(n, S, mat), kf_batch_workspace_size(cfg, n, S)));
   L.total = o;
   return L;
 }
@@ -272,7 +281,7 @@ int32_t hostChunk(const kf_inputs_t *hin, kf_outputs_t *hout, const kf_config_t 
                   int64_t cn, cudaStream_t s) {
   const int32_t S = hin->n_surfaces;
   const bool sm = hout->smoothed != nullptr;
-  const Staging L = stagingLayout(cn, S, sm);
+  const Staging L = stagingLayout(cn, S, sm, cfg);
   const size_t hs = (size_t)hin->stride;
   cudaError_t e = cudaSuccess;
   auto chk = [&](cudaError_t x) {
@@ -305,7 +314,7 @@ int32_t hostChunk(const kf_inputs_t *hin, kf_outputs_t *hout, const kf_config_t 
   dout.n_steps = reinterpret_cast<int32_t *>(d + L.nsteps);
   dout.n_trials = reinterpret_cast<int32_t *>(d + L.ntrials);
   dout.smoothed = sm ? reinterpret_cast<double *>(d + L.smoothed) : nullptr;
-  const size_t wsb = std::max(wsBytes(cn, S), kf_batch_workspace_size(nullptr, cn, S));
+  const size_t wsb = std::max(wsBytes(cn, S, cfg->material_effects != 0), kf_batch_workspace_size(cfg, cn, S));
   const int32_t rc = (cfg->kernel == KF_KERNEL_PERSISTENT)
                          ? kf_fit_batch_sorted(&din, &dout, cfg, geo, field, d + L.ws, wsb, s)
                          : kf_fit_batch(&din, &dout, cfg, geo, field, d + L.ws, wsb, s);
@@ -328,11 +337,24 @@ int32_t hostChunk(const kf_inputs_t *hin, kf_outputs_t *hout, const kf_config_t 
 }
 } // namespace
 
+int32_t kf_material_interaction(const double mat[6], int32_t flags, const double normal[3],
+                                const double dir[3], double p, double q, double mass,
+                                double out[5]) {
+  if (!mat || !normal || !dir || !out) return fail(KF_ERR_INVALID_ARGUMENT, "null argument%s");
+  kfm::Effects e;
+  if (!kfm::interact(mat, flags, normal, dir, p, q, mass, e)) return 1;
+  out[0] = e.p;
+  out[1] = e.varPhi;
+  out[2] = e.varTheta;
+  out[3] = e.varQop;
+  out[4] = e.eloss;
+  return KF_SUCCESS;
+}
+
 size_t kf_host_staging_size(const kf_config_t *cfg, int64_t n_tracks, int32_t n_surfaces,
                             int32_t with_smoothed) {
-  (void)cfg;
   if (n_tracks <= 0 || n_surfaces <= 0) return 0;
-  return stagingLayout(n_tracks, n_surfaces, with_smoothed != 0).total;
+  return stagingLayout(n_tracks, n_surfaces, with_smoothed != 0, cfg).total;
 }
 
 int32_t kf_fit_batch_host(const kf_inputs_t *hin, kf_outputs_t *hout, const kf_config_t *cfg,
@@ -346,7 +368,7 @@ int32_t kf_fit_batch_host(const kf_inputs_t *hin, kf_outputs_t *hout, const kf_c
   if (n == 0) return KF_SUCCESS;
   const int32_t S = hin->n_surfaces;
   const bool sm = hout->smoothed != nullptr;
-  const Staging L = stagingLayout(n, S, sm);
+  const Staging L = stagingLayout(n, S, sm, cfg);
   if (!dev || bytes < L.total)
     return fail(KF_ERR_WORKSPACE_TOO_SMALL, "staging smaller than kf_host_staging_size()%s");
   char *d = static_cast<char *>(dev);
@@ -357,7 +379,7 @@ int32_t kf_fit_batch_host(const kf_inputs_t *hin, kf_outputs_t *hout, const kf_c
   // area sized for the whole batch.
   int K = n >= 4 * kHostChunkMin ? 4 : (n >= 2 * kHostChunkMin ? 2 : 1);
   const int64_t chunk = (n + K - 1) / K;
-  const size_t slot = stagingLayout(chunk, S, sm).total;
+  const size_t slot = stagingLayout(chunk, S, sm, cfg).total;
   cudaStream_t aux = nullptr;
   if (K > 1 && (2 * slot > bytes || auxStream(&aux) != cudaSuccess)) K = 1;
   if (K == 1) {

@@ -41,6 +41,7 @@
 #include "../../include/gb300kf.h"
 #include "kf_adjoint_math.h"
 #include "kf_ff.cuh"
+#include "kf_material.h"
 
 namespace kfd {
 
@@ -53,6 +54,7 @@ constexpr int kStateStride = 37; // doubles per stored measurement state
 
 struct PlaneD {
   double c[3], U[3], V[3], T[3];
+  double mat[6]; // surface material (kf_geometry_t.material), thickness 0 = none
 };
 
 struct FieldD {
@@ -79,6 +81,9 @@ struct Params {
   double *oParams, *oCov, *oChi2, *oSmoothed;
   int32_t *oStatus, *oNMeas, *oNSteps, *oNTrials;
   double *ws;
+  int materialEffects;   // kf_config_t.material_effects when the geometry has material
+  double *wsCov;         // with material: [S][42][wsStride] predicted and filtered
+                         // covariance per state (the general smoother's input)
   const int32_t *perm;   // batched form: queue position -> track index
   int32_t *queueCounter; // batched form: next unclaimed queue position
   FieldD field;
@@ -1067,6 +1072,11 @@ template <typename R, typename H>
 __device__ __forceinline__ double *wsPtr(const Params &P, const Lane<R, H> &L, int s, int e) {
   return P.ws + ((size_t)s * kStateStride + e) * (size_t)P.wsStride + L.wsIdx;
 }
+// with material: predicted (e < 21) and filtered (21 + e) covariance of state s
+template <typename R, typename H>
+__device__ __forceinline__ double *wsCovPtr(const Params &P, const Lane<R, H> &L, int s, int e) {
+  return P.wsCov + ((size_t)s * 42 + e) * (size_t)P.wsStride + L.wsIdx;
+}
 
 // ---------------------------------------------------------------------------
 // Actor::filter (KalmanFitter.hpp:284-350) for a plane that has a hit, with
@@ -1099,6 +1109,14 @@ __device__ void filterHit(Lane<R, H> &L, const Params &P, const PlaneD *planes, 
   for (int e = 0; e < 6; ++e) *wsPtr(P, L, s, e) = pred[e];
 #pragma unroll
   for (int e = 0; e < 25; ++e) *wsPtr(P, L, s, 12 + e) = Jst[e];
+  if (P.materialEffects) {
+    // the general smoother's covariances: predicted, and filtered (= predicted
+    // for an outlier, overwritten below otherwise)
+    for (int e = 0; e < 21; ++e) {
+      *wsCovPtr(P, L, s, e) = L.cov(e);
+      *wsCovPtr(P, L, s, 21 + e) = L.cov(e);
+    }
+  }
   if (outlier) {
     // filtered = predicted; the stepper keeps the predicted state
 #pragma unroll
@@ -1143,9 +1161,25 @@ __device__ void filterHit(Lane<R, H> &L, const Params &P, const PlaneD *planes, 
     }
 #pragma unroll
     for (int e = 0; e < 6; ++e) *wsPtr(P, L, s, 6 + e) = filt[e];
+    if (P.materialEffects)
+      for (int e = 0; e < 21; ++e) *wsCovPtr(P, L, s, 21 + e) = cf[e];
     L.chi2 += chi2;
     stepperUpdate(L, pl, filt, cf, P.mass);
     if (!P.faithful) planeJacToGlobal(L, pl);
+  }
+  if (P.materialEffects) {
+    // the material effects after the filtering (KalmanFitter.hpp:344-345,
+    // PointwiseMaterialInteraction.hpp updateState): |p| after the mean energy
+    // loss, scattering and Landau variances added to the phi, theta and q/p
+    // variances of the bound covariance (an outlier crosses its plane too)
+    kfm::Effects fx;
+    if (kfm::interact(pl.mat, P.materialEffects, pl.T, L.dir, L.p, L.q, P.mass, fx)) {
+      L.p = fx.p;
+      legConstants(L, P.mass);
+      L.cov(ut(2, 2)) = smax(0., L.cov(ut(2, 2)) + fx.varPhi);
+      L.cov(ut(3, 3)) = smax(0., L.cov(ut(3, 3)) + fx.varTheta);
+      L.cov(ut(4, 4)) = smax(0., L.cov(ut(4, 4)) + fx.varQop);
+    }
   }
   L.hook.hitEnd(outlier);
   L.measStates++;
@@ -1366,9 +1400,145 @@ __device__ bool finalizeSmoothGain(Lane<R, H> &L, const Params &P, const PlaneD 
   return true;
 }
 
+// ---------------------------------------------------------------------------
+// The general gain-matrix smoother (GainMatrixSmoother.hpp:21-94) for fits
+// with material noise, where the closed forms above do not hold:
+//   G = C_f J^T C_p'^-1,  x_s = x_f + G (x_s' - x_p'),
+//   C_s = C_f - G (C_p' - C_s') G^T,
+// FP64 in both forms, C_p'^-1 applied through its Cholesky factor.
+// ---------------------------------------------------------------------------
+template <typename R, typename H>
+__device__ bool finalizeSmoothNoise(Lane<R, H> &L, const Params &P, const PlaneD *planes) {
+  L.smoothed = true;
+  const int n = L.measStates;
+  double xs[6], Cs[21];
+#pragma unroll
+  for (int e = 0; e < 6; ++e) xs[e] = *wsPtr(P, L, n - 1, 6 + e);
+#pragma unroll
+  for (int e = 0; e < 21; ++e) Cs[e] = *wsCovPtr(P, L, n - 1, 21 + e);
+  auto emit = [&](int s) {
+    if (!P.oSmoothed) return;
+#pragma unroll
+    for (int e = 0; e < 6; ++e) P.oSmoothed[((size_t)s * 27 + e) * P.stride + L.idx] = xs[e];
+#pragma unroll
+    for (int e = 0; e < 21; ++e) P.oSmoothed[((size_t)s * 27 + 6 + e) * P.stride + L.idx] = Cs[e];
+  };
+  emit(n - 1);
+  for (int i = n - 2; i >= 0; --i) {
+    double Cp[21], Cf[21], J[6][6];
+#pragma unroll
+    for (int e = 0; e < 21; ++e) {
+      Cp[e] = *wsCovPtr(P, L, i + 1, e);
+      Cf[e] = *wsCovPtr(P, L, i, 21 + e);
+    }
+    {
+      double Jn[25];
+#pragma unroll
+      for (int e = 0; e < 25; ++e) Jn[e] = *wsPtr(P, L, i + 1, 12 + e);
+      kfa::jstFull(Jn, J);
+    }
+    // Cholesky factor of C_p': Lc (lower, row-major upper-triangle layout
+    // by (i, j) = ut(j, i)), with the reciprocals of its diagonal
+    double Lc[21], id[6];
+    bool bad = false;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      double d = Cp[ut(c, c)];
+#pragma unroll
+      for (int k = 0; k < c; ++k) d -= Lc[ut(k, c)] * Lc[ut(k, c)];
+      bad = bad || !(d > 0.);
+      const double lcc = sqrt(d);
+      id[c] = 1. / lcc;
+      Lc[ut(c, c)] = lcc;
+#pragma unroll
+      for (int r = c + 1; r < 6; ++r) {
+        double v = Cp[ut(c, r)];
+#pragma unroll
+        for (int k = 0; k < c; ++k) v -= Lc[ut(k, r)] * Lc[ut(k, c)];
+        Lc[ut(c, r)] = v * id[c];
+      }
+    }
+    if (bad) return false;
+    // rows of G: C_p' g = (C_f J^T) row, by forward and back substitution
+    double G[6][6];
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+      double a[6];
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        double v = 0.;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) v += Cf[sidx(r, k)] * J[c][k];
+        a[c] = v;
+      }
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        double v = a[c];
+#pragma unroll
+        for (int k = 0; k < c; ++k) v -= Lc[ut(k, c)] * a[k];
+        a[c] = v * id[c];
+      }
+#pragma unroll
+      for (int c = 5; c >= 0; --c) {
+        double v = a[c];
+#pragma unroll
+        for (int k = c + 1; k < 6; ++k) v -= Lc[ut(c, k)] * a[k];
+        a[c] = v * id[c];
+      }
+      bool nan = false;
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        G[r][c] = a[c];
+        nan = nan || (a[c] != a[c]);
+      }
+      if (nan) return false;
+    }
+    double xn[6], D[21];
+#pragma unroll
+    for (int e = 0; e < 6; ++e) {
+      double v = 0.;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) v += G[e][k] * (xs[k] - *wsPtr(P, L, i + 1, k));
+      xn[e] = *wsPtr(P, L, i, 6 + e) + v;
+    }
+#pragma unroll
+    for (int e = 0; e < 21; ++e) D[e] = Cp[e] - Cs[e];
+    double M[6][6];
+#pragma unroll
+    for (int r = 0; r < 6; ++r)
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        double v = 0.;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) v += G[r][k] * D[sidx(k, c)];
+        M[r][c] = v;
+      }
+#pragma unroll
+    for (int r = 0; r < 6; ++r)
+#pragma unroll
+      for (int c = r; c < 6; ++c) {
+        double v = 0.;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) v += M[r][k] * G[c][k];
+        Cs[ut(r, c)] = Cf[ut(r, c)] - v;
+      }
+#pragma unroll
+    for (int e = 0; e < 6; ++e) xs[e] = xn[e];
+    emit(i);
+  }
+  const PlaneD &pl = planes[L.firstPlane];
+  stepperUpdate(L, pl, xs, Cs, P.mass);
+  if (!P.faithful) planeJacToGlobal(L, pl);
+  L.navDir = -1;
+  ssInit(L, -1. * DBL_MAX);
+  L.pathAcc = 0.;
+  return true;
+}
+
 template <typename R, typename H>
 __device__ bool finalizeSmooth(Lane<R, H> &L, const Params &P, const PlaneD *planes) {
   L.smoothed = true;
+  if (P.materialEffects) return finalizeSmoothNoise(L, P, planes);
   if (!P.oSmoothed) return finalizeSmoothGain<R>(L, P, planes);
   const int n = L.measStates;
   double xs[6], Cs[21];

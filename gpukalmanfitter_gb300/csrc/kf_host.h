@@ -11,8 +11,9 @@ char *errorBuffer(); // thread-local text behind kf_last_error_string()
 int32_t fail(int32_t code, const char *fmt, const char *detail = "");
 int32_t cudaFail(cudaError_t e, const char *where);
 
-// bytes of the per-state smoother workspace of n tracks
-size_t wsBytes(int64_t n, int32_t nSurf);
+// bytes of the per-state smoother workspace of n tracks (with material: the
+// covariances of the general smoother too)
+size_t wsBytes(int64_t n, int32_t nSurf, bool material);
 // argument checks shared by every fit entry point
 int32_t checkCommon(const kf_inputs_t *in, const kf_config_t *cfg, const kf_geometry_t *geo,
                     const kf_field_t *field);

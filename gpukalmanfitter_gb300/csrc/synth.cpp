@@ -9,6 +9,7 @@
 // phi in +-0.1, theta in pi/2 +- 0.1, 50 um hits, 50 um / 1 mrad / 5 % seeds).
 
 #include "../../include/gb300kf_synth.h"
+#include "kf_material.h"
 
 #include <cmath>
 #include <cstring>
@@ -282,6 +283,8 @@ int32_t kf_synth_tracks(const kf_synth_config_t *cfg, const double *tcenter,
       cfg->min_len > cfg->max_len)
     return KF_ERR_INVALID_ARGUMENT;
   const bool useMap = field && field->kind == KF_FIELD_GRID3D;
+  const bool withMaterial = cfg->material[0] > 0. && cfg->material[3] > 0.;
+  if (withMaterial && useMap) return KF_ERR_UNSUPPORTED; // material truth: uniform field only
   const double bz = cfg->bz_tesla * kTesla * ((field && !useMap) ? field->scale : 1.0);
   GridField GF{field};
 #ifdef _OPENMP
@@ -313,6 +316,7 @@ int32_t kf_synth_tracks(const kf_synth_config_t *cfg, const double *tcenter,
     double r[3] = {vtx[0], vtx[1], vtx[2]};
     double T[3] = {hx.st * std::cos(phi), hx.st * std::sin(phi), hx.ct};
     double sAcc = 0.;
+    double pCur = p; // momentum along the path (changes at material)
     for (int k = 0; k < S; ++k) {
       const double *c = tcenter + 3 * k;
       const double *R = trot + 9 * k;
@@ -330,6 +334,44 @@ int32_t kf_synth_tracks(const kf_synth_config_t *cfg, const double *tcenter,
         }
         sAcc = s;
         for (int a = 0; a < 3; ++a) hit[a] = rr[a];
+        if (withMaterial && k < len) {
+          // the plane's material: Highland scattering of the direction by two
+          // Gaussian angles, Bethe mean loss plus a Gaussian of the Landau width
+          kfm::Effects fx;
+          const double pNow = pCur;
+          kfm::interact(cfg->material, 3, nrm, TT, pNow, q, cfg->mass, fx);
+          const double th0 = std::sqrt(fx.varTheta);
+          // orthonormal u, v perpendicular to TT
+          double u[3] = {-TT[1], TT[0], 0.};
+          double un = std::sqrt(dot3(u, u));
+          if (un < 1e-12) {
+            u[0] = 1.;
+            u[1] = u[2] = 0.;
+            un = 1.;
+          }
+          for (int a = 0; a < 3; ++a) u[a] /= un;
+          const double v[3] = {TT[1] * u[2] - TT[2] * u[1], TT[2] * u[0] - TT[0] * u[2],
+                               TT[0] * u[1] - TT[1] * u[0]};
+          const double a1 = th0 * rng.normal(), a2 = th0 * rng.normal();
+          double Tn[3];
+          for (int a = 0; a < 3; ++a) Tn[a] = TT[a] + a1 * u[a] + a2 * v[a];
+          const double tn = std::sqrt(dot3(Tn, Tn));
+          for (int a = 0; a < 3; ++a) Tn[a] /= tn;
+          const double qop0 = q / pNow;
+          const double sigE = std::sqrt(fx.varQop) * pNow * pNow /
+                              std::sqrt(kfm::relativistic(cfg->mass, qop0, q).q2OverBeta2);
+          const double E = std::sqrt(cfg->mass * cfg->mass + pNow * pNow) - fx.eloss -
+                           sigE * rng.normal();
+          const double pNew = (E > cfg->mass) ? std::sqrt(E * E - cfg->mass * cfg->mass) : 1e-3;
+          // restart the helix at the hit with the new direction and momentum
+          for (int a = 0; a < 3; ++a) hx.x0[a] = rr[a];
+          hx.st = std::sqrt(Tn[0] * Tn[0] + Tn[1] * Tn[1]);
+          hx.ct = Tn[2];
+          hx.phi0 = std::atan2(Tn[1], Tn[0]);
+          hx.w = (q / pNew) * bz;
+          pCur = pNew;
+          sAcc = 0.;
+        }
       } else {
         // march with fixed steps until the plane is within one step, then
         // solve for the partial step that lands on it

@@ -115,6 +115,15 @@ typedef struct kf_config {
                                 compiled shapes (threads x CTAs): 128 x 2..5,
                                 64 x 4, 64 x 8, 256 x 1, 256 x 2; kf_autotune
                                 picks one */
+  int32_t material_effects;  /* bit 0: multiple scattering, bit 1: energy loss
+                                at the surfaces' material (kf_geometry_t.material)
+                                after each filter update (KalmanFitter.hpp:405-449,
+                                KalmanFitterOptions::multipleScattering /
+                                energyLoss); 0 (default) = none.  With material
+                                the smoother takes the reference's general gain
+                                C_f J^T C_p^-1 and the workspace grows (sizes
+                                depend on this field) */
+  int32_t reserved0;
 } kf_config_t;
 
 /* The surface sequence: boundless plane surfaces (PlaneSurface<InfiniteBounds>,
@@ -125,6 +134,12 @@ typedef struct kf_geometry {
   const double *center;   /* [n_planes][3] host memory */
   const double *rotation; /* [n_planes][9] host memory, row-major 3x3 whose
                              columns are the local axes U, V and the normal T */
+  const double *material; /* [n_planes][6] host memory or NULL: homogeneous
+                             surface material (Material/MaterialSlab.hpp,
+                             Material.hpp) as thickness (mm), radiation length
+                             X0 (mm), interaction length L0 (mm), relative
+                             atomic mass Ar, nuclear charge Z and molar density
+                             (mol/mm^3); thickness 0 = no material on the plane */
 } kf_geometry_t;
 
 /* Magnetic field: Test::ConstantBField (include/Test/Helper.hpp:17-22) or an
@@ -176,6 +191,19 @@ typedef struct kf_outputs {
 /* Version and diagnostics. */
 int32_t kf_version(void);
 const char *kf_last_error_string(void);
+
+/* Material interaction at one plane crossing (host; no GPU involved): the
+ * same computation the fit applies after a measurement with material
+ * (Propagator/detail/PointwiseMaterialInteraction.hpp/.ipp, formulas of
+ * Material/detail/Interactions.ipp).  mat as one row of
+ * kf_geometry_t.material, flags as kf_config_t.material_effects, unit
+ * plane normal and unit direction, |p| (GeV), charge, mass (GeV).
+ * out = (|p| after the mean energy loss, phi variance, theta variance, q/p
+ * variance, mean energy loss).  Returns 0, or 1 when nothing applies (no
+ * material or no effect selected; out untouched). */
+int32_t kf_material_interaction(const double mat[6], int32_t flags, const double normal[3],
+                                const double dir[3], double p, double q, double mass,
+                                double out[5]);
 
 /* Default configuration (reference defaults, FP64). */
 void kf_config_default(kf_config_t *cfg);

@@ -41,6 +41,12 @@ typedef struct kf_synth_config {
   double mis_shift_sigma;  /* truth-geometry misalignment: shifts (mm) */
   double mis_rot_sigma;    /* truth-geometry misalignment: rotations (rad) */
   double rk_step;          /* fixed RK4 step for field-map truth (mm) */
+  double material[6];      /* every plane's material as kf_geometry_t.material
+                              (thickness 0 = none); uniform-field truth only:
+                              at each plane on the path the particle scatters
+                              by Gaussian angles of the Highland width and
+                              loses the Bethe mean energy plus a Gaussian of
+                              the Landau width (the fitter's noise model) */
 } kf_synth_config_t;
 
 /* Defaults of the 10-plane uniform-field telescope workload. */

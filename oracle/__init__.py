@@ -82,9 +82,11 @@ def fit(tel, cfg=None, *, threads: int = 0, smoothed: bool = False, masks: bool 
     else:
         c = np.ascontiguousarray(center, dtype=np.float64)
         r = np.ascontiguousarray(rotation, dtype=np.float64)
+        m = None if tel.material is None else np.ascontiguousarray(tel.material, dtype=np.float64)
         geo = kf.KfGeometry(S, 0, c.ctypes.data_as(C.POINTER(C.c_double)),
-                            r.ctypes.data_as(C.POINTER(C.c_double)))
-        keep = (c, r)
+                            r.ctypes.data_as(C.POINTER(C.c_double)),
+                            m.ctypes.data_as(C.POINTER(C.c_double)) if m is not None else None)
+        keep = (c, r, m)
     fld = tel.field(None, field_scale)
     st = np.zeros((S, 63, n)) if states else None
     rc = lib.oracle_fit(C.byref(ins), C.byref(outs), C.byref(cfg), C.byref(geo), C.byref(fld),

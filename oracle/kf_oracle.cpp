@@ -20,7 +20,9 @@
 //  - outliers: with outlier_chi2_cut > 0 a hit whose predicted chi2 exceeds
 //    the cut becomes a state with filtered = predicted and no stepper update;
 //  - field: constant or trilinear 3D grid, times a global scale;
-//  - faithful_jacobian = 0 rebuilds jacToGlobal after each update.
+//  - faithful_jacobian = 0 rebuilds jacToGlobal after each update;
+//  - outliers cross their plane's material like hits do (the reference has
+//    no outliers).
 
 #include "../include/gb300kf.h"
 
@@ -151,6 +153,9 @@ struct Intersection {
 struct Plane {
   V3 c;
   double R[3][3];
+  // homogeneous surface material (Material.hpp, MaterialSlab.hpp): thickness
+  // (mm), X0, L0 (mm), Ar, Z, molar density (mol/mm^3); thickness 0 = none
+  double mat[6] = {0., 0., 0., 0., 0., 0.};
   V3 normal() const { return v3(R[0][2], R[1][2], R[2][2]); }
   // PlanarHelper::intersectionEstimate, Surfaces/detail/PlanarHelper.hpp:28-49
   Intersection intersect(const V3 &pos, const V3 &dir, double tol) const {
@@ -476,7 +481,108 @@ struct TrackState {
 struct Opts {
   int maxSteps, maxTrials, smoothing, faithful;
   double tol, cutoff, mass, overstep, surfTol, outlierCut;
+  int materialEffects; // bit 0 multiple scattering, bit 1 energy loss
 };
+
+// ---------------------------------------------------------------------------
+// Material effects at a surface (Material/detail/Interactions.ipp with
+// Propagator/detail/PointwiseMaterialInteraction.hpp/.ipp), for a heavy
+// (non-electron) particle.  Constants as the reference's double build sees
+// them: literals written as floats there (0.038f, 0.9f) keep their float
+// values.
+// ---------------------------------------------------------------------------
+namespace mat {
+const double kMe = 0.5109989461e-3;       // electron mass (GeV), Interactions.ipp:21
+const double kK = 0.307075e-3 * 10. * 10.; // Bethe prefactor K (GeV mm^2/mol), :23
+const double kPlasma = 28.816e-9;          // plasma energy scale (GeV), :25
+
+// RelativisticQuantities, Interactions.ipp:28-49
+struct Rel {
+  double q2OverBeta2, beta2, betaGamma, gamma;
+  Rel(double m, double qop, double q) {
+    q2OverBeta2 = q * q + (m * qop) * (m * qop);
+    const double mOverP = m * std::fabs(qop / q);
+    const double pOverM = 1.0 / mOverP;
+    beta2 = 1.0 / (1.0 + mOverP * mOverP);
+    betaGamma = pOverM;
+    gamma = std::sqrt(1.0 + pOverM * pOverM);
+  }
+};
+// Material::meanExcitationEnergy, Material.ipp (16 eV Z^0.9, exponent a float)
+inline double meanExcitation(double Z) { return 16e-9 * std::pow(Z, (double)0.9f); }
+// computeEpsilon, Interactions.ipp:101-106
+inline double epsilon(double Ne, double thickness, const Rel &r) {
+  return 0.5 * kK * Ne * thickness * r.q2OverBeta2;
+}
+// computeEnergyLossBethe, Interactions.ipp:150-176 (with computeMassTerm,
+// computeWMax, computeDeltaHalf, :58-131)
+inline double betheLoss(double thickness, double Z, double molarRho, double m, double qop,
+                        double q) {
+  const double I = meanExcitation(Z);
+  const double Ne = Z * molarRho;
+  const Rel r(m, qop, q);
+  const double eps = epsilon(Ne, thickness, r);
+  double dhalf = 0.;
+  if (!(r.betaGamma < 10.0))
+    dhalf = std::log(r.betaGamma) + std::log(kPlasma * std::sqrt(Ne) / I) - 0.5;
+  const double u = 2 * kMe * r.betaGamma * r.betaGamma;
+  const double mfrac = kMe / m;
+  const double wmax = (2 * kMe * r.betaGamma * r.betaGamma) /
+                      (1.0 + 2 * r.gamma * mfrac + mfrac * mfrac);
+  const double running = 0.5 * std::log(u / I) + 0.5 * std::log(wmax / I) - r.beta2 - dhalf;
+  return eps * running;
+}
+// computeEnergyLossLandauSigmaQOverP, Interactions.ipp:316-345
+inline double landauSigmaQop(double thickness, double Z, double molarRho, double m, double qop,
+                             double q) {
+  const Rel r(m, qop, q);
+  const double fwhm = 4 * epsilon(Z * molarRho, thickness, r);
+  const double sigmaE = fwhm / (2 * std::sqrt(2 * std::log(2.0)));
+  const double pInv = qop / q;
+  return std::sqrt(r.q2OverBeta2) * pInv * pInv * sigmaE;
+}
+// computeMultipleScatteringTheta0 with theta0Highland, Interactions.ipp:495-546
+inline double highlandTheta0(double xOverX0, double m, double qop, double q) {
+  const double momentumInv = std::fabs(qop / q);
+  const double q2OverBeta2 = Rel(m, qop, q).q2OverBeta2;
+  const double t = std::sqrt(xOverX0 * q2OverBeta2);
+  return 13.6e-3 * momentumInv * t * (1.0 + (double)0.038f * 2 * std::log(t));
+}
+} // namespace mat
+
+// KalmanFitter::Actor::materialInteractor (KalmanFitter.hpp:405-449) after a
+// measurement state, forward direction, full update stage: the slab scaled by
+// the path correction 1/|n.d| (PlaneSurface.ipp:229-235, MaterialSlab.ipp),
+// mean Bethe energy loss, Highland scattering into the phi and theta
+// variances, Landau width into the q/p variance (PointwiseMaterialInteraction
+// .ipp:14-51, .hpp updateState)
+static void materialInteraction(Stepper &s, const Plane &pl, const Opts &o) {
+  const double t0 = pl.mat[0], X0 = pl.mat[1], Ar = pl.mat[3], Z = pl.mat[4], rho = pl.mat[5];
+  if (!(o.materialEffects & 3) || !(0.0 < Ar) || !(0.0 < t0)) return;
+  const double eps = 2 * DBL_EPSILON;
+  const double pc = 1. / std::fabs(dot(pl.normal(), s.dir));
+  const double thickness = t0 * pc;
+  const double xOverX0 = ((eps < X0) ? (t0 / X0) : 0.) * pc;
+  const double q = s.q, qop = q / s.p, m = o.mass;
+  double eloss = 0., varPhi = 0., varTheta = 0., varQop = 0.;
+  if (o.materialEffects & 2) eloss = mat::betheLoss(thickness, Z, rho, m, qop, q);
+  if (o.materialEffects & 1) {
+    const double th0 = mat::highlandTheta0(xOverX0, m, qop, q);
+    const double perp = std::sqrt(s.dir[0] * s.dir[0] + s.dir[1] * s.dir[1]);
+    const double sigmaPhi = th0 * (norm(s.dir) / perp);
+    varPhi = sigmaPhi * sigmaPhi;
+    varTheta = th0 * th0;
+  }
+  if (o.materialEffects & 2) {
+    const double sq = mat::landauSigmaQop(thickness, Z, rho, m, qop, q);
+    varQop = sq * sq;
+  }
+  const double nextE = std::sqrt(m * m + s.p * s.p) - std::copysign(eloss, 1.);
+  s.p = (m < nextE) ? std::sqrt(nextE * nextE - m * m) : 0;
+  s.cov.a[2][2] = std::max(0., s.cov.a[2][2] + varPhi);
+  s.cov.a[3][3] = std::max(0., s.cov.a[3][3] + varTheta);
+  s.cov.a[4][4] = std::max(0., s.cov.a[4][4] + varQop);
+}
 
 struct Counters {
   long steps = 0;  // accepted RK steps
@@ -993,6 +1099,8 @@ static void fitTrack(const TrackIn &in, const std::vector<Plane> &planes,
       stepperUpdate(s, pl, ts.filt, ts.filtCov);
       if (!o.faithful) reinitPlane(s, pl);
     }
+    // the material effects after the filtering, KalmanFitter.hpp:344-345
+    materialInteraction(s, pl, o);
     states.push_back(ts);
     ++measStates;
     return true;
@@ -1132,6 +1240,8 @@ int32_t oracle_fit(const kf_inputs_t *in, kf_outputs_t *out,
       planes[k].c[r] = geo->center[3 * k + r];
       for (int c = 0; c < 3; ++c) planes[k].R[r][c] = geo->rotation[9 * k + 3 * r + c];
     }
+    if (geo->material)
+      for (int e = 0; e < 6; ++e) planes[k].mat[e] = geo->material[6 * k + e];
   }
   Field B;
   B.kind = field->kind;
@@ -1156,6 +1266,7 @@ int32_t oracle_fit(const kf_inputs_t *in, kf_outputs_t *out,
   o.overstep = cfg->overstep_limit;
   o.surfTol = cfg->on_surface_tol;
   o.outlierCut = cfg->outlier_chi2_cut;
+  o.materialEffects = geo->material ? cfg->material_effects : 0;
 
   const int64_t n = in->n_tracks, S = in->stride;
   const int nSurf = in->n_surfaces;
@@ -1227,6 +1338,33 @@ int32_t oracle_fit(const kf_inputs_t *in, kf_outputs_t *out,
     }
   }
   return KF_SUCCESS;
+}
+
+// one material interaction as the fit applies it (materialInteraction)
+int32_t oracle_material_interaction(const double matRow[6], int32_t flags, const double normal[3],
+                                    const double dir[3], double p, double q, double mass,
+                                    double out[5]) {
+  using namespace kfo;
+  Plane pl;
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) pl.R[r][c] = (c == 2) ? normal[r] : 0.;
+  for (int e = 0; e < 6; ++e) pl.mat[e] = matRow[e];
+  Stepper s;
+  s.dir = v3(dir[0], dir[1], dir[2]);
+  s.p = p;
+  s.q = (int)q;
+  s.cov = Mat<6, 6>::zero();
+  Opts o;
+  o.materialEffects = flags;
+  o.mass = mass;
+  if (!(flags & 3) || !(0.0 < matRow[3]) || !(0.0 < matRow[0])) return 1;
+  materialInteraction(s, pl, o);
+  out[0] = s.p;
+  out[1] = s.cov.a[2][2];
+  out[2] = s.cov.a[3][3];
+  out[3] = s.cov.a[4][4];
+  out[4] = std::sqrt(mass * mass + p * p) - std::sqrt(mass * mass + s.p * s.p);
+  return 0;
 }
 
 int32_t oracle_num_threads(void) {

@@ -98,7 +98,9 @@ def test_alignment_gradient_matches_finite_differences(ab):
                 al = np.zeros((ab.tel.n_surfaces, 6))
                 al[k, a] = d
                 return ab.run(grad=False, alignment=al)["chi2_total"][0]
-            fd = _fd4(f, 1e-4 * ALIGN_SCALE[a])
+            # 3e-4 of the scale: at 1e-4 the rotation differences of the total
+            # chi2 (8e4) scatter by ~1e-6 relative around the adjoint value
+            fd = _fd4(f, 3e-4 * ALIGN_SCALE[a])
             rels.append(abs(ga[k, a] - fd) / max(abs(fd), 1e-3 * np.max(np.abs(ga[:, a]))))
     rels = np.array(rels)
     assert np.median(rels) < 1e-7 and np.max(rels) < 1e-6, np.sort(rels)[-5:]
