@@ -57,6 +57,9 @@ WORKLOADS = {
                 "hit probability 0.9, 2 % outliers shifted U(+-5 mm), outlier chi2 cut 25",
                 dict(n_planes=30, x_first=50., x_step=50., min_len=5, max_len=30, hit_prob=0.9,
                      outlier_prob=0.02), dict(outlier_chi2_cut=25.0)),
+    "material10": ("telescope of 10 planes x=100..1000 mm, uniform 2 T, 0.5 mm silicon per plane "
+                   "(Highland scattering, Bethe loss, Landau width in the fit and in the truth)",
+                   dict(material=0.5), dict(material_effects=3)),
 }
 PRECISIONS = {"fp64": 0, "mixed": 1}
 # chi2 adjoint workload: truth planes misaligned, the fit uses the nominal geometry
@@ -395,6 +398,8 @@ def run_gpu(args) -> None:
                                                  [("batched_mixed", "mixed"), ("batched_fp64", "fp64")]),
             "differentiation": lambda: adjoint_entry(kf, max(1, n * 262144 // 1000000),
                                                      1234567894, stream, barrier, 3, 3),
+            "material": lambda: suite_entry(kf, "material10", n, 1234567895, stream, barrier, 3, 3,
+                                            [("batched_fp64", "fp64"), ("batched_mixed", "mixed")]),
         }
         suite = {k: makers[k]() for k in makers if k in wanted}
 
@@ -550,7 +555,7 @@ def main() -> None:
     ap.add_argument("--block-size", type=int, default=128, choices=[64, 128, 256],
                     help="batched form with --ctas-per-sm: threads per CTA; compiled "
                          "shapes 128 x 2..5, 64 x 4, 64 x 8, 256 x 1, 256 x 2")
-    ap.add_argument("--suite", default="batching,precision_map,differentiation",
+    ap.add_argument("--suite", default="batching,precision_map,differentiation,material",
                     help="comma list of suite entries to run (or 'none')")
     args = ap.parse_args()
     if args.warmup < 3:

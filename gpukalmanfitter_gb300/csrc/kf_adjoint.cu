@@ -62,6 +62,7 @@ struct AdjParams {
 __device__ __forceinline__ double hdr(int type, int len) { return (double)(type * 65536 + len); }
 
 struct TapeHook {
+  static constexpr bool kMaterial = false;
   double *tape;
   int32_t *info;
   int64_t n;

@@ -55,6 +55,10 @@ cudaError_t launchPersistent_mixed_256_1(const kfd::Params &, cudaStream_t);
 cudaError_t launchPersistent_mixed_256_1_prep();
 cudaError_t launchPersistent_mixed_256_2(const kfd::Params &, cudaStream_t);
 cudaError_t launchPersistent_mixed_256_2_prep();
+cudaError_t launchPersistent_fp64_mat(const kfd::Params &, cudaStream_t);
+cudaError_t launchPersistent_fp64_mat_prep();
+cudaError_t launchPersistent_mixed_mat(const kfd::Params &, cudaStream_t);
+cudaError_t launchPersistent_mixed_mat_prep();
 
 namespace {
 
@@ -84,8 +88,20 @@ const Variant kVariants[] = {
     {KF_PRECISION_MIXED, 256, 2, launchPersistent_mixed_256_2, launchPersistent_mixed_256_2_prep},
 };
 
+// with material effects: the one instantiation with the material code
+// (128 threads, 4 CTAs per SM), whatever the shape fields say
+const Variant kMaterialVariants[] = {
+    {KF_PRECISION_FP64, 128, 4, launchPersistent_fp64_mat, launchPersistent_fp64_mat_prep},
+    {KF_PRECISION_MIXED, 128, 4, launchPersistent_mixed_mat, launchPersistent_mixed_mat_prep},
+};
+
 // the instantiation for a configuration (block size 0/128, min blocks 0 = 4)
 const Variant *findVariant(const kf_config_t *cfg) {
+  if (cfg->material_effects) {
+    for (const Variant &v : kMaterialVariants)
+      if (v.precision == cfg->precision) return &v;
+    return nullptr;
+  }
   const int bs = cfg->block_size ? cfg->block_size : 128;
   const int mb = cfg->min_blocks_per_sm ? cfg->min_blocks_per_sm : 4;
   for (const Variant &v : kVariants)
@@ -313,6 +329,8 @@ int32_t kf_autotune(const kf_inputs_t *in, kf_outputs_t *out, const kf_config_t 
   int32_t rc = KF_SUCCESS;
   for (const Variant &v : kVariants) {
     if (v.precision != cfg->precision) continue;
+    // with material effects the one material instantiation (128 x 4) runs
+    if (cfg->material_effects && (v.bs != 128 || v.minb != 4)) continue;
     kf_config_t c = *cfg;
     c.kernel = KF_KERNEL_PERSISTENT;
     c.block_size = v.bs;

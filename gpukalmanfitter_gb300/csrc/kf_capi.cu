@@ -21,6 +21,8 @@ using namespace kfd;
 // two compile in parallel)
 cudaError_t launchFitFp64(const kfd::Params &P, unsigned grid, cudaStream_t s);
 cudaError_t launchFitMixed(const kfd::Params &P, unsigned grid, cudaStream_t s);
+cudaError_t launchFitFp64Mat(const kfd::Params &P, unsigned grid, cudaStream_t s);
+cudaError_t launchFitMixedMat(const kfd::Params &P, unsigned grid, cudaStream_t s);
 
 namespace {
 thread_local char g_err[512] = "";
@@ -134,7 +136,7 @@ void fillParams(Params &P, const kf_inputs_t *in, const kf_outputs_t *out, const
       pl.V[r] = geo->rotation[9 * k + 3 * r + 1];
       pl.T[r] = geo->rotation[9 * k + 3 * r + 2];
     }
-    for (int e = 0; e < 6; ++e) pl.mat[e] = geo->material ? geo->material[6 * k + e] : 0.;
+    for (int e = 0; e < 6; ++e) P.planeMat[k][e] = geo->material ? geo->material[6 * k + e] : 0.;
   }
   P.materialEffects = (geo->material && cfg->material_effects) ? (cfg->material_effects & 3) : 0;
   P.wsCov = cfg->material_effects
@@ -152,8 +154,10 @@ int32_t launchFit(const Params &P, int precision, int blockSize, cudaStream_t s)
   (void)blockSize;
   if (P.n == 0) return KF_SUCCESS;
   const unsigned grid = (unsigned)((P.n + kFitBlock - 1) / kFitBlock);
-  cudaError_t e = (precision == KF_PRECISION_MIXED) ? launchFitMixed(P, grid, s)
-                                                    : launchFitFp64(P, grid, s);
+  const bool mat = P.materialEffects != 0;
+  cudaError_t e = (precision == KF_PRECISION_MIXED)
+                      ? (mat ? launchFitMixedMat(P, grid, s) : launchFitMixed(P, grid, s))
+                      : (mat ? launchFitFp64Mat(P, grid, s) : launchFitFp64(P, grid, s));
   if (e == cudaSuccess) e = cudaGetLastError();
   if (e != cudaSuccess) return cudaFail(e, "fit kernel launch");
   return KF_SUCCESS;

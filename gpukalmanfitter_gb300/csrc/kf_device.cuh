@@ -54,7 +54,6 @@ constexpr int kStateStride = 37; // doubles per stored measurement state
 
 struct PlaneD {
   double c[3], U[3], V[3], T[3];
-  double mat[6]; // surface material (kf_geometry_t.material), thickness 0 = none
 };
 
 struct FieldD {
@@ -88,6 +87,7 @@ struct Params {
   int32_t *queueCounter; // batched form: next unclaimed queue position
   FieldD field;
   PlaneD planes[KF_MAX_PLANES];
+  double planeMat[KF_MAX_PLANES][6]; // surface material (kf_geometry_t.material)
 };
 
 // upper-triangle index of (i, j), i <= j, row-major
@@ -222,12 +222,20 @@ template <typename R> __host__ __device__ constexpr size_t coldStateBytes(int th
 // Recording hook of a lane: the fit kernels use NoHook (every call compiles
 // to nothing); the chi2 adjoint records its tape through these calls.
 struct NoHook {
+  static constexpr bool kMaterial = false; // surface material code compiled in
   template <class LT> __device__ __forceinline__ void stepBegin(const LT &) {}
   template <class LT> __device__ __forceinline__ void trial(const LT &, double) {}
   template <class LT> __device__ __forceinline__ void stepEnd(const LT &, bool) {}
   template <class LT> __device__ __forceinline__ void actorSet(const LT &, int) {}
   template <class LT> __device__ __forceinline__ void hitBegin(const LT &, int) {}
   __device__ __forceinline__ void hitEnd(bool) {}
+};
+
+// the fit kernels for geometries with material (kf_config_t.material_effects):
+// the same lane program with the material interaction and the general smoother
+// compiled in (the others carry none of that code)
+struct MaterialHook : NoHook {
+  static constexpr bool kMaterial = true;
 };
 
 template <typename R, typename H = NoHook> struct Lane {
@@ -1085,6 +1093,12 @@ __device__ __forceinline__ double *wsCovPtr(const Params &P, const Lane<R, H> &L
 // (I - KH) C (I - KH)^T + K V K^T, which stays positive definite when the
 // predicted covariance carries FP32-level errors from the Jacobian.
 // ---------------------------------------------------------------------------
+// the material interaction at plane k (material kernels only)
+static __device__ __forceinline__ bool materialStep(const Params &P, int k, const double dir[3], double p,
+                                          double q, kfm::Effects &fx) {
+  return kfm::interact(P.planeMat[k], P.materialEffects, P.planes[k].T, dir, p, q, P.mass, fx);
+}
+
 template <typename R, typename H>
 __device__ void filterHit(Lane<R, H> &L, const Params &P, const PlaneD *planes, int k) {
   const PlaneD &pl = planes[k];
@@ -1109,7 +1123,7 @@ __device__ void filterHit(Lane<R, H> &L, const Params &P, const PlaneD *planes, 
   for (int e = 0; e < 6; ++e) *wsPtr(P, L, s, e) = pred[e];
 #pragma unroll
   for (int e = 0; e < 25; ++e) *wsPtr(P, L, s, 12 + e) = Jst[e];
-  if (P.materialEffects) {
+  if (H::kMaterial && P.materialEffects) {
     // the general smoother's covariances: predicted, and filtered (= predicted
     // for an outlier, overwritten below otherwise)
     for (int e = 0; e < 21; ++e) {
@@ -1161,24 +1175,26 @@ __device__ void filterHit(Lane<R, H> &L, const Params &P, const PlaneD *planes, 
     }
 #pragma unroll
     for (int e = 0; e < 6; ++e) *wsPtr(P, L, s, 6 + e) = filt[e];
-    if (P.materialEffects)
+    if (H::kMaterial && P.materialEffects)
       for (int e = 0; e < 21; ++e) *wsCovPtr(P, L, s, 21 + e) = cf[e];
     L.chi2 += chi2;
     stepperUpdate(L, pl, filt, cf, P.mass);
     if (!P.faithful) planeJacToGlobal(L, pl);
   }
-  if (P.materialEffects) {
+  if constexpr (H::kMaterial) {
+    if (P.materialEffects) {
     // the material effects after the filtering (KalmanFitter.hpp:344-345,
     // PointwiseMaterialInteraction.hpp updateState): |p| after the mean energy
     // loss, scattering and Landau variances added to the phi, theta and q/p
     // variances of the bound covariance (an outlier crosses its plane too)
     kfm::Effects fx;
-    if (kfm::interact(pl.mat, P.materialEffects, pl.T, L.dir, L.p, L.q, P.mass, fx)) {
+    if (materialStep(P, k, L.dir, L.p, L.q, fx)) {
       L.p = fx.p;
       legConstants(L, P.mass);
       L.cov(ut(2, 2)) = smax(0., L.cov(ut(2, 2)) + fx.varPhi);
       L.cov(ut(3, 3)) = smax(0., L.cov(ut(3, 3)) + fx.varTheta);
       L.cov(ut(4, 4)) = smax(0., L.cov(ut(4, 4)) + fx.varQop);
+    }
     }
   }
   L.hook.hitEnd(outlier);
@@ -1407,34 +1423,33 @@ __device__ bool finalizeSmoothGain(Lane<R, H> &L, const Params &P, const PlaneD 
 //   C_s = C_f - G (C_p' - C_s') G^T,
 // FP64 in both forms, C_p'^-1 applied through its Cholesky factor.
 // ---------------------------------------------------------------------------
-template <typename R, typename H>
-__device__ bool finalizeSmoothNoise(Lane<R, H> &L, const Params &P, const PlaneD *planes) {
-  L.smoothed = true;
-  const int n = L.measStates;
-  double xs[6], Cs[21];
+// Compiled into the material kernels only (MaterialHook).  u: the track's
+// workspace column, i: its track index (outputs), n: states.
+static __device__ __forceinline__ bool smoothNoise(const Params &P, int64_t u, int64_t i_, int n,
+                                         double xs[6], double Cs[21]) {
+  auto WS = [&](int s, int e) { return P.ws[((size_t)s * kStateStride + e) * (size_t)P.wsStride + u]; };
+  auto WC = [&](int s, int e) { return P.wsCov[((size_t)s * 42 + e) * (size_t)P.wsStride + u]; };
 #pragma unroll
-  for (int e = 0; e < 6; ++e) xs[e] = *wsPtr(P, L, n - 1, 6 + e);
+  for (int e = 0; e < 6; ++e) xs[e] = WS(n - 1, 6 + e);
 #pragma unroll
-  for (int e = 0; e < 21; ++e) Cs[e] = *wsCovPtr(P, L, n - 1, 21 + e);
+  for (int e = 0; e < 21; ++e) Cs[e] = WC(n - 1, 21 + e);
   auto emit = [&](int s) {
     if (!P.oSmoothed) return;
-#pragma unroll
-    for (int e = 0; e < 6; ++e) P.oSmoothed[((size_t)s * 27 + e) * P.stride + L.idx] = xs[e];
-#pragma unroll
-    for (int e = 0; e < 21; ++e) P.oSmoothed[((size_t)s * 27 + 6 + e) * P.stride + L.idx] = Cs[e];
+    for (int e = 0; e < 6; ++e) P.oSmoothed[((size_t)s * 27 + e) * P.stride + i_] = xs[e];
+    for (int e = 0; e < 21; ++e) P.oSmoothed[((size_t)s * 27 + 6 + e) * P.stride + i_] = Cs[e];
   };
   emit(n - 1);
   for (int i = n - 2; i >= 0; --i) {
     double Cp[21], Cf[21], J[6][6];
 #pragma unroll
     for (int e = 0; e < 21; ++e) {
-      Cp[e] = *wsCovPtr(P, L, i + 1, e);
-      Cf[e] = *wsCovPtr(P, L, i, 21 + e);
+      Cp[e] = WC(i + 1, e);
+      Cf[e] = WC(i, 21 + e);
     }
     {
       double Jn[25];
 #pragma unroll
-      for (int e = 0; e < 25; ++e) Jn[e] = *wsPtr(P, L, i + 1, 12 + e);
+      for (int e = 0; e < 25; ++e) Jn[e] = WS(i + 1, 12 + e);
       kfa::jstFull(Jn, J);
     }
     // Cholesky factor of C_p': Lc (lower, row-major upper-triangle layout
@@ -1498,8 +1513,8 @@ __device__ bool finalizeSmoothNoise(Lane<R, H> &L, const Params &P, const PlaneD
     for (int e = 0; e < 6; ++e) {
       double v = 0.;
 #pragma unroll
-      for (int k = 0; k < 6; ++k) v += G[e][k] * (xs[k] - *wsPtr(P, L, i + 1, k));
-      xn[e] = *wsPtr(P, L, i, 6 + e) + v;
+      for (int k = 0; k < 6; ++k) v += G[e][k] * (xs[k] - WS(i + 1, k));
+      xn[e] = WS(i, 6 + e) + v;
     }
 #pragma unroll
     for (int e = 0; e < 21; ++e) D[e] = Cp[e] - Cs[e];
@@ -1526,19 +1541,23 @@ __device__ bool finalizeSmoothNoise(Lane<R, H> &L, const Params &P, const PlaneD
     for (int e = 0; e < 6; ++e) xs[e] = xn[e];
     emit(i);
   }
-  const PlaneD &pl = planes[L.firstPlane];
-  stepperUpdate(L, pl, xs, Cs, P.mass);
-  if (!P.faithful) planeJacToGlobal(L, pl);
-  L.navDir = -1;
-  ssInit(L, -1. * DBL_MAX);
-  L.pathAcc = 0.;
   return true;
 }
 
 template <typename R, typename H>
 __device__ bool finalizeSmooth(Lane<R, H> &L, const Params &P, const PlaneD *planes) {
   L.smoothed = true;
-  if (P.materialEffects) return finalizeSmoothNoise(L, P, planes);
+  if (H::kMaterial && P.materialEffects) {
+    double xs[6], Cs[21];
+    if (!smoothNoise(P, L.wsIdx, L.idx, L.measStates, xs, Cs)) return false;
+    const PlaneD &pl = planes[L.firstPlane];
+    stepperUpdate(L, pl, xs, Cs, P.mass);
+    if (!P.faithful) planeJacToGlobal(L, pl);
+    L.navDir = -1;
+    ssInit(L, -1. * DBL_MAX);
+    L.pathAcc = 0.;
+    return true;
+  }
   if (!P.oSmoothed) return finalizeSmoothGain<R>(L, P, planes);
   const int n = L.measStates;
   double xs[6], Cs[21];

@@ -29,9 +29,9 @@ template <typename R> struct MinBlocks {
 
 // Fit the tracks i (inputs/outputs) with workspace columns w of one warp;
 // i < 0 marks an idle lane.  All 32 lanes must call it together.
-template <typename R>
+template <typename R, typename H>
 __device__ __forceinline__ void fitWarp(const Params &P, const PlaneD *sp, int64_t i, int64_t w) {
-  Lane<R> L;
+  Lane<R, H> L;
   initLane(L, P, sp, i, w);
   for (;;) {
     if (!L.parked && L.pc != PC_DONE) advance(L, P, sp);
@@ -54,16 +54,16 @@ __device__ __forceinline__ void fitWarp(const Params &P, const PlaneD *sp, int64
   }
 }
 
-template <int BS, int MINB, typename R>
+template <int BS, int MINB, typename R, typename H = NoHook>
 __global__ void __launch_bounds__(BS, MINB) fitGrid(const __grid_constant__ Params P) {
   __shared__ PlaneD sp[KF_MAX_PLANES];
   for (int k = threadIdx.x; k < P.nSurf; k += BS) sp[k] = P.planes[k];
   __syncthreads();
   const int64_t i = (int64_t)blockIdx.x * BS + threadIdx.x;
-  fitWarp<R>(P, sp, i, i);
+  fitWarp<R, H>(P, sp, i, i);
 }
 
-template <int BS, int MINB, typename R>
+template <int BS, int MINB, typename R, typename H = NoHook>
 __global__ void __launch_bounds__(BS, MINB) fitPersistent(const __grid_constant__ Params P) {
   __shared__ PlaneD sp[KF_MAX_PLANES];
   for (int k = threadIdx.x; k < P.nSurf; k += BS) sp[k] = P.planes[k];
@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(BS, MINB) fitPersistent(const __grid_constant_
     if ((int64_t)base >= P.n) break;
     const int64_t q = (int64_t)base + lane;
     const int64_t i = (q < P.n) ? (int64_t)P.perm[q] : -1;
-    fitWarp<R>(P, sp, i, q < P.n ? q : 0);
+    fitWarp<R, H>(P, sp, i, q < P.n ? q : 0);
   }
 }
 
@@ -86,9 +86,10 @@ __global__ void __launch_bounds__(BS, MINB) fitPersistent(const __grid_constant_
 // device holds at once (occupancy query), never more than the batch needs.
 // NAME##_prep lifts the CTA's dynamic shared-memory limit to the cold state's
 // size (needed above 48 KB); callers run it before any launch or capture.
-#define KF_PERSISTENT_LAUNCHER(NAME, BS, MINB, R)                                              \
+#define KF_PERSISTENT_LAUNCHER(NAME, BS, MINB, R) KF_PERSISTENT_LAUNCHER_H(NAME, BS, MINB, R, kfd::NoHook)
+#define KF_PERSISTENT_LAUNCHER_H(NAME, BS, MINB, R, H)                                         \
   cudaError_t NAME##_prep() {                                                                \
-    return cudaFuncSetAttribute(kfd::fitPersistent<BS, MINB, R>,                             \
+    return cudaFuncSetAttribute(kfd::fitPersistent<BS, MINB, R, H>,                          \
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,                 \
                                 (int)kfd::coldStateBytes<R>(BS));                            \
   }                                                                                          \
@@ -98,13 +99,13 @@ __global__ void __launch_bounds__(BS, MINB) fitPersistent(const __grid_constant_
     if (e != cudaSuccess) return e;                                                          \
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);                   \
     if (e != cudaSuccess) return e;                                                          \
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kfd::fitPersistent<BS, MINB, R>, \
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kfd::fitPersistent<BS, MINB, R, H>, \
                                                       BS, kfd::coldStateBytes<R>(BS));       \
     if (e != cudaSuccess) return e;                                                          \
     int64_t blocks = (int64_t)sms * (per > 0 ? per : 1);                                     \
     const int64_t need = (P.n + BS - 1) / BS;                                                \
     if (blocks > need) blocks = need;                                                        \
     if (blocks < 1) blocks = 1;                                                              \
-    kfd::fitPersistent<BS, MINB, R><<<(unsigned)blocks, BS, kfd::coldStateBytes<R>(BS), s>>>(P); \
+    kfd::fitPersistent<BS, MINB, R, H><<<(unsigned)blocks, BS, kfd::coldStateBytes<R>(BS), s>>>(P); \
     return cudaGetLastError();                                                               \
   }

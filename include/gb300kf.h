@@ -122,7 +122,9 @@ typedef struct kf_config {
                                 energyLoss); 0 (default) = none.  With material
                                 the smoother takes the reference's general gain
                                 C_f J^T C_p^-1 and the workspace grows (sizes
-                                depend on this field) */
+                                depend on this field); the batched form runs its
+                                material instantiation (128 threads x 4 CTAs per
+                                SM) whatever the shape fields say */
   int32_t reserved0;
 } kf_config_t;
 
