@@ -57,9 +57,20 @@ struct MagneticFieldContext {};
 
 /// Boundless plane surface with the reference's curvilinear frame:
 /// T = normal, U = z x T (x x T near z), V = T x U.
+/// Homogeneous surface material (Material/MaterialSlab.hpp, Material.hpp):
+/// thickness (mm), X0, L0 (mm), Ar, Z, molar density (mol/mm^3).
+struct MaterialSlab {
+  double thickness = 0., X0 = 0., L0 = 0., Ar = 0., Z = 0., molarDensity = 0.;
+  /// silicon as Test/Helper.hpp:25-29 builds it
+  static MaterialSlab silicon(double thicknessMm) {
+    return {thicknessMm, 93.70, 465.2, 28.0855, 14., (2.329 / 28.0855) / 1000.};
+  }
+};
+
 class PlaneSurface {
 public:
-  PlaneSurface(const Vector3D &center, const Vector3D &normal) : m_center(center) {
+  PlaneSurface(const Vector3D &center, const Vector3D &normal, MaterialSlab material = {})
+      : m_center(center), m_material(material) {
     double n = std::sqrt(normal[0] * normal[0] + normal[1] * normal[1] + normal[2] * normal[2]);
     Vector3D T{normal[0] / n, normal[1] / n, normal[2] / n};
     Vector3D a = (std::fabs(T[2]) < 0.999995) ? Vector3D{0, 0, 1} : Vector3D{1, 0, 0};
@@ -77,12 +88,14 @@ public:
   GeometryID geoID() const { return m_id; }
   const Vector3D &center() const { return m_center; }
   const std::array<double, 9> &rotation() const { return m_rot; }
+  const MaterialSlab &material() const { return m_material; }
 
 private:
   static Vector3D cross(const Vector3D &a, const Vector3D &b) {
     return {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
   }
   Vector3D m_center;
+  MaterialSlab m_material;
   std::array<double, 9> m_rot{};
   GeometryID m_id{};
 };
@@ -151,6 +164,8 @@ struct KalmanFitterOptions {
   double outlierChi2Cut = 0.; // 0: no outlier rejection (reference VoidOutlierFinder)
   bool batched = false;       // fitBatch: length-sorted persistent kernel (batched form)
   bool mixedPrecision = false; // FP32 propagation and Jacobian transport, FP64 Kalman algebra
+  bool multipleScattering = true; // at surfaces with material (KalmanFitter.hpp:92)
+  bool energyLoss = true;         // at surfaces with material (KalmanFitter.hpp:95)
 };
 
 struct KalmanFitterResult {
@@ -224,7 +239,14 @@ public:
     const int S = static_cast<int>(nSurfaces);
     results.assign(tracks.size(), KalmanFitterResult());
     if (n == 0) return;
-    std::vector<double> center(3 * S), rot(9 * S);
+    std::vector<double> center(3 * S), rot(9 * S), mat(6 * S);
+    bool anyMaterial = false;
+    for (int k = 0; k < S; ++k) {
+      const MaterialSlab &m = surfaces[k].material();
+      const double row[6] = {m.thickness, m.X0, m.L0, m.Ar, m.Z, m.molarDensity};
+      for (int e = 0; e < 6; ++e) mat[6 * k + e] = row[e];
+      anyMaterial = anyMaterial || (m.thickness > 0. && m.Ar > 0.);
+    }
     for (int k = 0; k < S; ++k) {
       for (int r = 0; r < 3; ++r) center[3 * k + r] = surfaces[k].center()[r];
       for (int e = 0; e < 9; ++e) rot[9 * k + e] = surfaces[k].rotation()[e];
@@ -287,7 +309,9 @@ public:
     cfg.outlier_chi2_cut = kfOptions.outlierChi2Cut;
     cfg.kernel = kfOptions.batched ? KF_KERNEL_PERSISTENT : KF_KERNEL_THREAD_PER_TRACK;
     cfg.precision = kfOptions.mixedPrecision ? KF_PRECISION_MIXED : KF_PRECISION_FP64;
-    kf_geometry_t geo{S, 0, center.data(), rot.data()};
+    if (anyMaterial)
+      cfg.material_effects = (kfOptions.multipleScattering ? 1 : 0) | (kfOptions.energyLoss ? 2 : 0);
+    kf_geometry_t geo{S, 0, center.data(), rot.data(), anyMaterial ? mat.data() : nullptr};
     kf_field_t field{};
     field.kind = KF_FIELD_CONSTANT;
     field.scale = 1.;
