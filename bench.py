@@ -8,12 +8,14 @@ seeds smeared by 50 um / 1 mrad / 5 %.  Synthetic, seeded, generated on the
 host.  One step = one fit of the whole batch: in the batched form (default)
 one CUDA-graph launch (work-queue sort + persistent fit kernel, shape picked
 by the autotuner beforehand), in the plain form one grid kernel launch.  The
-line carries both forms on the same batch ("forms"), and a suite of two more
-one-GPU comparisons: 4M uneven tracks with holes and outliers on 30 planes,
-1M tracks on 30 planes in the FP32 field map (plain FP64 against batched FP64
-and batched mixed precision), and the chi2 adjoint (gradients with respect to
-plane alignment, start parameters and field scale) on 256k tracks of a
-misaligned 20-plane telescope against one forward fit of the same batch.
+line carries both forms on the same batch ("forms"), and a suite of one-GPU
+comparisons: 4M uneven tracks with holes and outliers on 30 planes, 1M tracks
+on 30 planes in the FP32 field map (plain FP64 against batched FP64 and
+batched mixed precision), the chi2 adjoint (gradients with respect to plane
+alignment, start parameters and field scale) on 256k tracks of a misaligned
+20-plane telescope against one forward fit of the same batch, 1M tracks
+through 0.5 mm of silicon per plane (material effects), and the output
+writers (params CSV, states obj, params table) on 256k fitted tracks.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
                   [--form batched|plain] [--workload W] [--precision fp64|mixed]
@@ -311,6 +313,43 @@ def adjoint_entry(kf, n: int, seed: int, stream, barrier, steps: int, warmup: in
             "checkpoint_every_states": 5}
 
 
+def output_entry(kf, n: int, seed: int, stream) -> dict:
+    """The output writers (gb300kf_io.h, Run/Common/Writer.hpp) on one fitted
+    batch with smoothed states: host seconds per file, written to a scratch
+    directory that is removed afterwards."""
+    import os
+    import shutil
+    import tempfile
+    import torch
+    from gpukalmanfitter_gb300 import writer
+    tel = make_workload(kf, "uniform10", n, seed)
+    with torch.cuda.stream(stream):
+        b = kf.DeviceBatch(tel, fit_config(kf, "uniform10", "fp64"), smoothed=True)
+    b.fit(stream)
+    stream.synchronize()
+    res = {k: v for k, v in b.results().items()}
+    del b
+    torch.cuda.empty_cache()
+    d = tempfile.mkdtemp(prefix="kf_out_")
+    out = {"workload": "uniform10: the headline telescope, smoothed states kept", "tracks": n,
+           "threads": os.cpu_count()}
+    try:
+        for name, fn in (("params_csv", lambda p: writer.write_params_csv(p, res)),
+                         ("states_obj", lambda p: writer.write_states_obj(p, res, tel)),
+                         ("params_table", lambda p: writer.write_params_table(p, res, tel))):
+            path = os.path.join(d, name)
+            fn(path)  # warm-up (page cache, thread pool)
+            t0 = time.perf_counter()
+            fn(path)
+            sec = time.perf_counter() - t0
+            size = os.path.getsize(path)
+            out[name] = {"seconds": sec, "tracks_per_s": n / sec, "mb": size / 1e6,
+                         "mb_per_s": size / 1e6 / sec}
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    return out
+
+
 def run_gpu(args) -> None:
     import torch
     import gpukalmanfitter_gb300 as kf
@@ -400,6 +439,7 @@ def run_gpu(args) -> None:
                                                      1234567894, stream, barrier, 3, 3),
             "material": lambda: suite_entry(kf, "material10", n, 1234567895, stream, barrier, 3, 3,
                                             [("batched_fp64", "fp64"), ("batched_mixed", "mixed")]),
+            "output": lambda: output_entry(kf, max(1, n * 262144 // 1000000), 1234567896, stream),
         }
         suite = {k: makers[k]() for k in makers if k in wanted}
 
@@ -555,7 +595,7 @@ def main() -> None:
     ap.add_argument("--block-size", type=int, default=128, choices=[64, 128, 256],
                     help="batched form with --ctas-per-sm: threads per CTA; compiled "
                          "shapes 128 x 2..5, 64 x 4, 64 x 8, 256 x 1, 256 x 2")
-    ap.add_argument("--suite", default="batching,precision_map,differentiation,material",
+    ap.add_argument("--suite", default="batching,precision_map,differentiation,material,output",
                     help="comma list of suite entries to run (or 'none')")
     args = ap.parse_args()
     if args.warmup < 3:

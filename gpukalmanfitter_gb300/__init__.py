@@ -194,6 +194,11 @@ class Telescope:
     truth_rotation: np.ndarray | None = None
     misalignment: np.ndarray | None = None  # [S,6]
     material: np.ndarray | None = None      # [S,6] surface material (None: vacuum)
+    # a grid that is not the cube of field_n points over +-field_half (an
+    # ingested map, gpukalmanfitter_gb300.fieldmap): points and extent per axis
+    field_dims: tuple | None = None
+    field_min: tuple | None = None
+    field_max: tuple | None = None
 
     def geometry(self) -> tuple[KfGeometry, tuple]:
         c = np.ascontiguousarray(self.center, dtype=np.float64)
@@ -210,10 +215,16 @@ class Telescope:
             f.value[0], f.value[1], f.value[2] = 0.0, 0.0, self.bz_tesla * TESLA
         else:
             f.kind = 1
-            f.nx = f.ny = f.nz = self.field_n
-            for a in range(3):
-                f.min[a] = -self.field_half
-                f.max[a] = self.field_half
+            if self.field_dims is not None:
+                f.nx, f.ny, f.nz = self.field_dims
+                for a in range(3):
+                    f.min[a] = self.field_min[a]
+                    f.max[a] = self.field_max[a]
+            else:
+                f.nx = f.ny = f.nz = self.field_n
+                for a in range(3):
+                    f.min[a] = -self.field_half
+                    f.max[a] = self.field_half
             f.grid = grid_ptr if grid_ptr is not None else self.field_grid.ctypes.data
         return f
 
@@ -236,12 +247,15 @@ def synth_config(**kw) -> SynthConfig:
 def make_telescope(n: int, *, seed: int = 1234567890, n_planes: int = 10,
                    x_first: float = 100.0, x_step: float = 100.0, min_len: int | None = None,
                    max_len: int | None = None, hit_prob: float = 1.0,
-                   outlier_prob: float = 0.0, field_map: bool = False, field_n: int = 101,
+                   outlier_prob: float = 0.0, field_map=False, field_n: int = 101,
                    field_half: float = 1500.0, mis_shift: float = 0.0, mis_rot: float = 0.0,
                    material: float = 0.0, threads: int = 0, **extra) -> Telescope:
     """Seeded synthetic telescope workload (host arrays).  material > 0: every
     plane carries that many mm of silicon (the reference driver's 0.5 mm,
-    Run/GPU/KalmanFitterGPUTest.cu:253) in the geometry and in the truth."""
+    Run/GPU/KalmanFitterGPUTest.cu:253) in the geometry and in the truth.
+    field_map: True for the analytic map of field_n^3 points over
+    +-field_half, or a FieldMap (gpukalmanfitter_gb300.fieldmap) read from a
+    file; the truth and the fit then use that grid."""
     lib = load()
     cfg = synth_config(n_tracks=n, seed=seed, n_planes=n_planes, x_first=x_first, x_step=x_step,
                        min_len=min_len or n_planes, max_len=max_len or n_planes,
@@ -259,7 +273,10 @@ def make_telescope(n: int, *, seed: int = 1234567890, n_planes: int = 10,
                                  _ptr(trot), _ptr(align)))
     grid = None
     field = None
-    if field_map:
+    ingested = field_map is not None and not isinstance(field_map, bool)
+    if ingested:
+        grid = np.ascontiguousarray(field_map.grid, dtype=np.float32).reshape(-1)
+    elif field_map:
         grid = np.zeros(field_n ** 3 * 4, dtype=np.float32)
         _check(lib.kf_synth_field_map(C.c_double(cfg.bz_tesla), field_n, C.c_double(field_half),
                                       grid.ctypes.data))
@@ -269,7 +286,11 @@ def make_telescope(n: int, *, seed: int = 1234567890, n_planes: int = 10,
     tel = Telescope(n, S, center, rot, meas, mask, nplanes, start, scov, per, truth,
                     cfg.bz_tesla, grid, field_n if field_map else 0, field_half,
                     tcenter, trot, align, mat)
-    if field_map:
+    if ingested:
+        tel.field_dims = tuple(field_map.dims)
+        tel.field_min = tuple(field_map.min)
+        tel.field_max = tuple(field_map.max)
+    if field_map is not None and field_map is not False:
         field = tel.field()
     _check(lib.kf_synth_tracks(C.byref(cfg), _ptr(tcenter), _ptr(trot),
                                C.byref(field) if field is not None else None,

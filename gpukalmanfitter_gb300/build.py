@@ -25,7 +25,7 @@ CU_SOURCES = ["kf_capi.cu", "kf_fit_fp64.cu", "kf_fit_mixed.cu", "kf_fit_fp64_ma
               "kf_fit_mixed_mat.cu", "kf_batch.cu", "kf_diag.cu",
               "kf_noalloc.cu", "kf_adjoint.cu"] + [f"kf_tune_{p}_{m}.cu" for p in ("fp64", "mixed")
                                                      for m in ("2", "3", "5", "64x4", "64x8", "256x1", "256x2")]
-CXX_SOURCES = ["synth.cpp"]
+CXX_SOURCES = ["synth.cpp", "kf_io.cpp", "kf_fieldmap.cpp"]
 
 
 def _nvcc() -> str:

@@ -53,7 +53,8 @@ enum kf_error {
   KF_ERR_WORKSPACE_TOO_SMALL = -2,
   KF_ERR_CUDA = -3,
   KF_ERR_UNSUPPORTED = -4,
-  KF_ERR_NO_DEVICE = -5
+  KF_ERR_NO_DEVICE = -5,
+  KF_ERR_IO = -6 /* an output file could not be written (gb300kf_io.h) */
 };
 
 /* ---- per-track status (kf_outputs_t.status) ------------------------------ *

@@ -110,6 +110,36 @@ int main() {
     for (int e = 0; e < 6; ++e)
       if (bres[i].fittedParameters.parameters()[e] != res[i].fittedParameters.parameters()[e]) ++bad;
   }
+  // planes carrying 0.5 mm of silicon: the shim passes the slabs with the
+  // reference's default scattering and energy-loss options
+  std::vector<PlaneSurface> mplanes;
+  std::vector<double> mat(6 * S);
+  for (int k = 0; k < S; ++k) {
+    mplanes.emplace_back(Vector3D{100. * (k + 1), 0., 0.}, Vector3D{1., 0., 0.},
+                         MaterialSlab::silicon(0.5));
+    mplanes.back().assignGeoID(GeometryID{(uint64_t)(1000 + k)});
+    const MaterialSlab &m = mplanes.back().material();
+    const double row[6] = {m.thickness, m.X0, m.L0, m.Ar, m.Z, m.molarDensity};
+    for (int e = 0; e < 6; ++e) mat[6 * k + e] = row[e];
+  }
+  std::vector<KalmanFitterResult> mres;
+  fitter.fitBatch(tracks, opt, mres, mplanes.data(), mplanes.size());
+  kf_config_t mcfg = cfg;
+  mcfg.material_effects = 3;
+  kf_geometry_t mgeo{S, 0, center.data(), rot.data(), mat.data()};
+  const size_t mbytes = kf_host_staging_size(&mcfg, n, S, 0);
+  if (cudaMalloc(&dev, mbytes) != cudaSuccess) return 2;
+  if (kf_fit_batch_host(&in, &out, &mcfg, &mgeo, &field, dev, mbytes, nullptr) != 0) return 4;
+  cudaFree(dev);
+  int changed = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    if (mres[i].status != oSt[i] || mres[i].chi2 != oChi[i]) ++bad;
+    for (int e = 0; e < 6; ++e) {
+      if (mres[i].fittedParameters.parameters()[e] != oPar[e * n + i]) ++bad;
+      if (mres[i].fittedParameters.parameters()[e] != res[i].fittedParameters.parameters()[e]) ++changed;
+    }
+  }
+  if (changed < n) ++bad; // the material must change the fits
   std::printf("shim tracks=%lld mismatches=%d\n", (long long)n, bad);
   return bad == 0 ? 0 : 1;
 }
