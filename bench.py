@@ -14,8 +14,9 @@ on 30 planes in the FP32 field map (plain FP64 against batched FP64 and
 batched mixed precision), the chi2 adjoint (gradients with respect to plane
 alignment, start parameters and field scale) on 256k tracks of a misaligned
 20-plane telescope against one forward fit of the same batch, 1M tracks
-through 0.5 mm of silicon per plane (material effects), and the output
-writers (params CSV, states obj, params table) on 256k fitted tracks.
+through 0.5 mm of silicon per plane (material effects), the output writers
+(params CSV, states obj, params table) on 256k fitted tracks, and input
+production: 4M uneven tracks simulated on the GPU against the host generator.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
                   [--form batched|plain] [--workload W] [--precision fp64|mixed]
@@ -313,6 +314,48 @@ def adjoint_entry(kf, n: int, seed: int, stream, barrier, steps: int, warmup: in
             "checkpoint_every_states": 5}
 
 
+def simulation_entry(kf, n: int, seed: int, stream, barrier, host_sample: int) -> dict:
+    """Input production: the uneven 30-plane workload generated on the GPU
+    (kf_simulate_tracks, one thread per track, arrays written in HBM) against
+    the host generator (kf_synth_tracks, OpenMP over all host cores) on a
+    bounded sample of the same tracks; and the map workload's RK4 truth."""
+    import torch
+    _, kw, _ = WORKLOADS["holes30"]
+    with torch.cuda.stream(stream):
+        tel = kf.make_telescope(n, seed=seed, device="cuda", **kw)
+    ms, _ = timed_steps(lambda: tel.simulate(stream), stream, 3, 3, barrier)
+    out = {"workload": f"holes30: {WORKLOADS['holes30'][0]}", "tracks": n,
+           "gpu_tracks_per_s": n * 3 / (ms * 1e-3), "gpu_ms": ms / 3,
+           "bytes_written_per_track": 30 * 5 * 8 + 8 + 4 + (6 + 21 + 3 + 6) * 8}
+    out["gpu_write_gbs"] = out["bytes_written_per_track"] * out["gpu_tracks_per_s"] / 1e9
+    del tel
+    torch.cuda.empty_cache()
+    kf.make_telescope(1000, seed=seed, **kw)  # host warm-up (thread pool)
+    t0 = time.perf_counter()
+    kf.make_telescope(host_sample, seed=seed, **kw)
+    sec = time.perf_counter() - t0
+    out["host_tracks_per_s"] = host_sample / sec
+    out["host_sample_tracks"] = host_sample
+    out["host_threads"] = os.cpu_count()
+    out["gpu_over_host"] = out["gpu_tracks_per_s"] / out["host_tracks_per_s"]
+    # field-map truth (fixed-step RK4, 5 mm steps through the 101^3 map)
+    _, mkw, _ = WORKLOADS["map30"]
+    nm = max(1, n // 4)
+    with torch.cuda.stream(stream):
+        tm = kf.make_telescope(nm, seed=seed, device="cuda", **mkw)
+    ms, _ = timed_steps(lambda: tm.simulate(stream), stream, 3, 3, barrier)
+    out["map30_tracks"] = nm
+    out["map30_gpu_tracks_per_s"] = nm * 3 / (ms * 1e-3)
+    del tm
+    torch.cuda.empty_cache()
+    hm = max(1, host_sample // 10)
+    t0 = time.perf_counter()
+    kf.make_telescope(hm, seed=seed, **mkw)
+    out["map30_host_tracks_per_s"] = hm / (time.perf_counter() - t0)
+    out["map30_gpu_over_host"] = out["map30_gpu_tracks_per_s"] / out["map30_host_tracks_per_s"]
+    return out
+
+
 def output_entry(kf, n: int, seed: int, stream) -> dict:
     """The output writers (gb300kf_io.h, Run/Common/Writer.hpp) on one fitted
     batch with smoothed states: host seconds per file, written to a scratch
@@ -440,6 +483,8 @@ def run_gpu(args) -> None:
             "material": lambda: suite_entry(kf, "material10", n, 1234567895, stream, barrier, 3, 3,
                                             [("batched_fp64", "fp64"), ("batched_mixed", "mixed")]),
             "output": lambda: output_entry(kf, max(1, n * 262144 // 1000000), 1234567896, stream),
+            "simulation": lambda: simulation_entry(kf, 4 * n, 1234567897, stream, barrier,
+                                                   max(1, n // 5)),
         }
         suite = {k: makers[k]() for k in makers if k in wanted}
 
@@ -595,7 +640,8 @@ def main() -> None:
     ap.add_argument("--block-size", type=int, default=128, choices=[64, 128, 256],
                     help="batched form with --ctas-per-sm: threads per CTA; compiled "
                          "shapes 128 x 2..5, 64 x 4, 64 x 8, 256 x 1, 256 x 2")
-    ap.add_argument("--suite", default="batching,precision_map,differentiation,material,output",
+    ap.add_argument("--suite",
+                    default="batching,precision_map,differentiation,material,output,simulation",
                     help="comma list of suite entries to run (or 'none')")
     args = ap.parse_args()
     if args.warmup < 3:

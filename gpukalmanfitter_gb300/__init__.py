@@ -94,7 +94,7 @@ EXPORTS = ["kf_version", "kf_last_error_string", "kf_config_default", "kf_worksp
            "kf_fit_batch_sorted", "kf_batch_plan_create", "kf_batch_plan_launch",
            "kf_batch_plan_destroy", "kf_autotune",
            "kf_synth_config_default", "kf_synth_geometry", "kf_synth_field_map",
-           "kf_synth_tracks"]
+           "kf_synth_tracks", "kf_simulate_tracks"]
 
 
 def load(build_if_missing: bool = True) -> C.CDLL:
@@ -148,6 +148,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.kf_synth_field_map.restype = C.c_int32
     lib.kf_synth_field_map.argtypes = [C.c_double, C.c_int32, C.c_double, C.c_void_p]
     lib.kf_synth_tracks.restype = C.c_int32
+    lib.kf_simulate_tracks.restype = C.c_int32
     _LIB = lib
     return lib
 
@@ -199,6 +200,7 @@ class Telescope:
     field_dims: tuple | None = None
     field_min: tuple | None = None
     field_max: tuple | None = None
+    synth_cfg: object = None                # SynthConfig of a GPU-simulated telescope
 
     def geometry(self) -> tuple[KfGeometry, tuple]:
         c = np.ascontiguousarray(self.center, dtype=np.float64)
@@ -228,6 +230,36 @@ class Telescope:
             f.grid = grid_ptr if grid_ptr is not None else self.field_grid.ctypes.data
         return f
 
+    def simulate(self, stream=None) -> None:
+        """(Re)generate the tracks of a GPU-simulated telescope into its own
+        device arrays with kf_simulate_tracks on `stream` (asynchronous)."""
+        import torch
+        field = None
+        if self.field_grid is not None:
+            field = self.field(self.field_grid.data_ptr())
+        s = stream if stream is not None else torch.cuda.current_stream()
+        tc = np.ascontiguousarray(self.truth_center, dtype=np.float64)
+        tr = np.ascontiguousarray(self.truth_rotation, dtype=np.float64)
+        _check(load().kf_simulate_tracks(C.byref(self.synth_cfg), _ptr(tc), _ptr(tr),
+                                         C.byref(field) if field is not None else None,
+                                         *[C.c_void_p(a.data_ptr()) for a in
+                                           (self.meas, self.hit_mask, self.n_planes, self.start,
+                                            self.start_cov, self.perigee, self.truth)],
+                                         C.c_void_p(s.cuda_stream)))
+
+    def to_host(self) -> "Telescope":
+        """A copy whose per-track arrays (torch tensors of a GPU-simulated
+        telescope) are numpy arrays."""
+        import copy
+        t = copy.copy(self)
+        for k in ("meas", "hit_mask", "n_planes", "start", "start_cov", "perigee", "truth",
+                  "field_grid"):
+            v = getattr(self, k)
+            if v is not None and hasattr(v, "detach"):
+                a = v.detach().cpu().numpy()
+                setattr(t, k, a.view(np.uint64) if k == "hit_mask" else a)
+        return t
+
 
 def silicon(thickness_mm: float) -> np.ndarray:
     """Surface material row (thickness, X0, L0, Ar, Z, molar density) of
@@ -249,13 +281,17 @@ def make_telescope(n: int, *, seed: int = 1234567890, n_planes: int = 10,
                    max_len: int | None = None, hit_prob: float = 1.0,
                    outlier_prob: float = 0.0, field_map=False, field_n: int = 101,
                    field_half: float = 1500.0, mis_shift: float = 0.0, mis_rot: float = 0.0,
-                   material: float = 0.0, threads: int = 0, **extra) -> Telescope:
+                   material: float = 0.0, threads: int = 0, device: str | None = None,
+                   **extra) -> Telescope:
     """Seeded synthetic telescope workload (host arrays).  material > 0: every
     plane carries that many mm of silicon (the reference driver's 0.5 mm,
     Run/GPU/KalmanFitterGPUTest.cu:253) in the geometry and in the truth.
     field_map: True for the analytic map of field_n^3 points over
     +-field_half, or a FieldMap (gpukalmanfitter_gb300.fieldmap) read from a
-    file; the truth and the fit then use that grid."""
+    file; the truth and the fit then use that grid.  device ("cuda", ...):
+    the tracks are simulated on that GPU (kf_simulate_tracks, the same
+    tracks as the host generator's) and the per-track arrays are torch
+    tensors there (Telescope.to_host() gives the numpy form)."""
     lib = load()
     cfg = synth_config(n_tracks=n, seed=seed, n_planes=n_planes, x_first=x_first, x_step=x_step,
                        min_len=min_len or n_planes, max_len=max_len or n_planes,
@@ -280,9 +316,17 @@ def make_telescope(n: int, *, seed: int = 1234567890, n_planes: int = 10,
         grid = np.zeros(field_n ** 3 * 4, dtype=np.float32)
         _check(lib.kf_synth_field_map(C.c_double(cfg.bz_tesla), field_n, C.c_double(field_half),
                                       grid.ctypes.data))
-    meas = np.zeros((S, 5, n)); mask = np.zeros(n, dtype=np.uint64)
-    nplanes = np.zeros(n, dtype=np.int32); start = np.zeros((6, n)); scov = np.zeros((21, n))
-    per = np.zeros((3, n)); truth = np.zeros((6, n))
+    if device is not None:
+        import torch
+        z = lambda *shape, dt=torch.float64: torch.zeros(shape, dtype=dt, device=device)
+        meas, mask, nplanes = z(S, 5, n), z(n, dt=torch.int64), z(n, dt=torch.int32)
+        start, scov, per, truth = z(6, n), z(21, n), z(3, n), z(6, n)
+        if grid is not None:
+            grid = torch.from_numpy(grid).to(device)
+    else:
+        meas = np.zeros((S, 5, n)); mask = np.zeros(n, dtype=np.uint64)
+        nplanes = np.zeros(n, dtype=np.int32); start = np.zeros((6, n)); scov = np.zeros((21, n))
+        per = np.zeros((3, n)); truth = np.zeros((6, n))
     tel = Telescope(n, S, center, rot, meas, mask, nplanes, start, scov, per, truth,
                     cfg.bz_tesla, grid, field_n if field_map else 0, field_half,
                     tcenter, trot, align, mat)
@@ -291,7 +335,12 @@ def make_telescope(n: int, *, seed: int = 1234567890, n_planes: int = 10,
         tel.field_min = tuple(field_map.min)
         tel.field_max = tuple(field_map.max)
     if field_map is not None and field_map is not False:
-        field = tel.field()
+        field = tel.field(grid.data_ptr() if device is not None else None)
+    if device is not None:
+        import torch
+        tel.synth_cfg = cfg
+        tel.simulate(torch.cuda.current_stream(device))
+        return tel
     _check(lib.kf_synth_tracks(C.byref(cfg), _ptr(tcenter), _ptr(trot),
                                C.byref(field) if field is not None else None,
                                _ptr(meas), _ptr(mask, C.c_uint64), _ptr(nplanes, C.c_int32),
@@ -387,7 +436,7 @@ class DeviceBatch:
         self.tel = tel
         self.cfg = cfg or default_config()
         n, S = tel.n, tel.n_surfaces
-        t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)
+        t = lambda a: a if hasattr(a, "data_ptr") else torch.from_numpy(np.ascontiguousarray(a)).to(device)
         self.arrays = {k: (t(v) if v is not None else None) for k, v in tel_arrays(tel, masks).items()}
         self.out = {"params": torch.zeros((6, n), dtype=torch.float64, device=device),
                     "cov": torch.zeros((21, n), dtype=torch.float64, device=device),
@@ -522,7 +571,7 @@ class AdjointBatch:
         self.tel = tel
         self.cfg = cfg or default_config()
         n, S = tel.n, tel.n_surfaces
-        t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)
+        t = lambda a: a if hasattr(a, "data_ptr") else torch.from_numpy(np.ascontiguousarray(a)).to(device)
         self.arrays = {k: (t(v) if v is not None else None) for k, v in tel_arrays(tel, True).items()}
         self.out = {"chi2": torch.zeros(n, dtype=torch.float64, device=device),
                     "status": torch.zeros(n, dtype=torch.int32, device=device),

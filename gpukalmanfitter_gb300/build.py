@@ -23,9 +23,13 @@ LIB = LIBDIR / "libgb300kf.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["kf_capi.cu", "kf_fit_fp64.cu", "kf_fit_mixed.cu", "kf_fit_fp64_mat.cu",
               "kf_fit_mixed_mat.cu", "kf_batch.cu", "kf_diag.cu",
-              "kf_noalloc.cu", "kf_adjoint.cu"] + [f"kf_tune_{p}_{m}.cu" for p in ("fp64", "mixed")
+              "kf_noalloc.cu", "kf_adjoint.cu", "kf_sim.cu"] + [f"kf_tune_{p}_{m}.cu" for p in ("fp64", "mixed")
                                                      for m in ("2", "3", "5", "64x4", "64x8", "256x1", "256x2")]
 CXX_SOURCES = ["synth.cpp", "kf_io.cpp", "kf_fieldmap.cpp"]
+# The simulation kernel runs the host generator's per-track code; without
+# contraction into FMA on either side the two differ only by the math
+# library's rounding (the host side is built with -ffp-contract=off).
+CU_EXTRA_FLAGS = {"kf_sim.cu": ["-fmad=false"]}
 
 
 def _nvcc() -> str:
@@ -65,13 +69,14 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     nvcc = _nvcc()
     cu_flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                        "-I", str(INCLUDE)]
-    cxx_flags = ["-O2", "-std=c++17", "-fPIC", "-fopenmp", "-I", str(INCLUDE)]
+    cxx_flags = ["-O2", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-I", str(INCLUDE)]
     jobs = []
     objs = []
     for s in CU_SOURCES:
         o = obj / (Path(s).stem + ".o")
         objs.append(o)
-        jobs.append([nvcc, *cu_flags, "-c", str(CSRC / s), "-o", str(o)])
+        jobs.append([nvcc, *cu_flags, *CU_EXTRA_FLAGS.get(s, []), "-c", str(CSRC / s), "-o",
+                     str(o)])
     for s in CXX_SOURCES:
         o = obj / (Path(s).stem + ".o")
         objs.append(o)

@@ -76,6 +76,19 @@ int32_t kf_synth_tracks(const kf_synth_config_t *cfg, const double *truth_center
                         double *start_params, double *start_cov,
                         double *perigee, double *truth, int32_t n_threads);
 
+/* The same tracks generated on the GPU: one thread per track runs the
+ * per-track code of kf_synth_tracks, so every random draw, hit, hole,
+ * outlier and length is the host generator's, and the values agree with it
+ * to the last-bit rounding of the math library.  Output arrays and
+ * `field->grid` are DEVICE memory; truth_center / truth_rotation are host
+ * arrays (copied into the launch).  Asynchronous on `stream` (a
+ * cudaStream_t, NULL = legacy default stream); nothing is allocated. */
+int32_t kf_simulate_tracks(const kf_synth_config_t *cfg, const double *truth_center,
+                           const double *truth_rotation, const kf_field_t *field,
+                           double *meas, uint64_t *hit_mask, int32_t *n_planes,
+                           double *start_params, double *start_cov, double *perigee,
+                           double *truth, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
