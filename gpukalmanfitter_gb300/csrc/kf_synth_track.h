@@ -251,6 +251,10 @@ KFS_HD inline void simulateTrack(const kf_synth_config_t &cfg, const double *tce
     const double *c = tcenter + 3 * k;
     const double *R = trot + 9 * k;
     const double nrm[3] = {R[2], R[5], R[8]};
+    // Newton stops when the correction is within rounding of the plane's
+    // distance from the origin (an absolute 1e-13 mm is below one ulp there
+    // and would run every iteration on rounding noise)
+    const double tolS = 1e-12 * (1.0 + fabs(dot3(nrm, c)));
     double hit[3];
     if (!useMap) {
       double s = sAcc, rr[3], TT[3];
@@ -260,7 +264,7 @@ KFS_HD inline void simulateTrack(const kf_synth_config_t &cfg, const double *tce
         const double ds = -dot3(nrm, d) / dot3(nrm, TT);
         s += ds;
         hx.at(s, rr, TT);
-        if (fabs(ds) < 1e-13) break;
+        if (fabs(ds) < tolS) break;
       }
       sAcc = s;
       for (int a = 0; a < 3; ++a) hit[a] = rr[a];
@@ -328,7 +332,7 @@ KFS_HD inline void simulateTrack(const kf_synth_config_t &cfg, const double *tce
         const double d[3] = {ro[0] - c[0], ro[1] - c[1], ro[2] - c[2]};
         const double dh = -dot3(nrm, d) / dot3(nrm, To);
         h += dh;
-        if (fabs(dh) < 1e-13) break;
+        if (fabs(dh) < tolS) break;
       }
       rk4(*F, qop, r, T, h, ro, To);
       for (int a = 0; a < 3; ++a) {
