@@ -36,8 +36,9 @@ extern "C" int32_t kf_simulate_tracks(const kf_synth_config_t *cfg, const double
                                       double *meas, uint64_t *hit_mask, int32_t *n_planes,
                                       double *start_params, double *start_cov, double *perigee,
                                       double *truth, void *stream) {
-  if (!cfg || !truth_center || !truth_rotation || !meas || !start_params || !start_cov ||
-      !perigee)
+  if (!cfg) return kfh::fail(KF_ERR_INVALID_ARGUMENT, "kf_simulate_tracks: %s", "no config");
+  if (cfg->n_tracks == 0) return KF_SUCCESS; // nothing to write (arrays may be NULL)
+  if (!truth_center || !truth_rotation || !meas || !start_params || !start_cov || !perigee)
     return kfh::fail(KF_ERR_INVALID_ARGUMENT, "kf_simulate_tracks: %s", "missing array");
   const int S = cfg->n_planes;
   if (cfg->n_tracks < 0 || S <= 0 || S > KF_MAX_PLANES || cfg->min_len < 1 ||
@@ -52,7 +53,6 @@ extern "C" int32_t kf_simulate_tracks(const kf_synth_config_t *cfg, const double
   if (useMap && (!field->grid || ((uintptr_t)field->grid & 15) || field->nx < 2 ||
                  field->ny < 2 || field->nz < 2))
     return kfh::fail(KF_ERR_INVALID_ARGUMENT, "kf_simulate_tracks: %s", "bad field grid");
-  if (cfg->n_tracks == 0) return KF_SUCCESS;
   SimParams P;
   P.cfg = *cfg;
   for (int k = 0; k < 3 * S; ++k) P.tcenter[k] = truth_center[k];

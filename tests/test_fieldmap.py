@@ -208,3 +208,20 @@ def test_gpu_fit_in_ingested_map(kf, orc, tmp_path):
     sig = np.sqrt(np.abs(o["cov"][[0, 6, 11, 15, 18, 20]]))[:, ok]
     rel = np.abs(g["params"][:, ok] - o["params"][:, ok]) / np.maximum(np.abs(o["params"][:, ok]), sig)
     assert np.all(np.median(rel, axis=1) <= 1e-6)
+
+
+def test_two_point_axes_and_zero_padding(tmp_path):
+    """The smallest map (2 points per axis): 3 grid points per axis, the top
+    plane zero, and the lookup halfway into the padded cell is half the
+    last point's value (the reference's fall to zero)."""
+    from oracle import field_map as OF
+    x = y = z = np.array([0., 10.])
+    b = np.ones((2, 2, 2, 3)) * np.array([0.1, 0.2, 2.0])
+    p = tmp_path / "tiny.txt"
+    FM.write_field_map_xyz(p, x, y, z, b, fmt="%.17g")
+    fm = FM.read_field_map_xyz(p)
+    assert fm.dims == (3, 3, 3) and fm.max == (20., 20., 20.)
+    assert np.all(fm.grid[2] == 0) and np.all(fm.grid[:, 2] == 0) and np.all(fm.grid[:, :, 2] == 0)
+    a = OF.trilinear(fm.grid, fm.dims, fm.min, fm.max, [5., 5., 15.])
+    r = OF.MapXYZ(p, field_unit=TESLA).field([5., 5., 15.])
+    assert np.allclose(a, r, rtol=1e-6) and np.allclose(a[2], 1.0 * TESLA, rtol=1e-6)

@@ -70,3 +70,11 @@ def test_simulation_rejects_bad_arguments(kf):
         kf.make_telescope(10, seed=1, device="cuda", min_len=5, max_len=3)
     with pytest.raises(kf.KfError):
         kf.make_telescope(10, seed=1, device="cuda", material=0.5, field_map=True, field_n=11)
+
+
+def test_zero_tracks_and_one_track(kf):
+    t0 = kf.make_telescope(0, seed=3, device="cuda")
+    assert t0.meas.shape[2] == 0
+    h = kf.make_telescope(1, seed=3)
+    d = kf.make_telescope(1, seed=3, device="cuda").to_host()
+    assert np.array_equal(h.hit_mask, d.hit_mask) and np.array_equal(h.truth, d.truth)

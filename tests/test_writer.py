@@ -144,3 +144,29 @@ def test_resolution_report(tmp_path, kf, orc):
         assert abs(rep[name]["pull"]["mean"]) < 0.1, (name, rep[name])
         assert 0.9 < rep[name]["pull"]["sigma"] < 1.1, (name, rep[name])
     assert rep["eLOC0"]["residual_rms"] < 0.1
+
+
+def test_empty_and_all_failed(tmp_path, kf):
+    """No tracks, or no fitted track: the CSV files hold their header only,
+    the obj files are empty (the reference writes the header and skips every
+    unsuccessful fit)."""
+    from oracle import writers as ow
+    for n in (0, 5):
+        res = {"params": np.zeros((6, n)), "cov": np.ones((21, n)),
+               "status": np.full(n, 3, dtype=np.int32), "n_meas": np.zeros(n, dtype=np.int32),
+               "smoothed": np.zeros((10, 27, n))}
+        tel = kf.make_telescope(max(n, 1), seed=1)
+        if n == 0:
+            tel.hit_mask = tel.hit_mask[:0]
+            tel.truth = np.zeros((6, 0))
+            tel.perigee = np.zeros((3, 0))
+        p = tmp_path / f"p{n}.csv"
+        writer.write_params_csv(p, res)
+        assert p.read_text() == ow.params_csv(res["params"], res["status"])
+        assert p.read_text().count("\n") == 1
+        o = tmp_path / f"s{n}.obj"
+        writer.write_states_obj(o, res, tel)
+        assert o.read_text() == ""
+        t = tmp_path / f"t{n}.csv"
+        writer.write_params_table(t, res, tel)
+        assert t.read_text().count("\n") == 1
