@@ -49,7 +49,8 @@ struct AdjParams {
   double *xs;        // [S][6][n] smoothed parameters (by position)
   int32_t *info;     // [S][n] plane index | outlier << 8 (by position)
   double *snap;      // [nCk][kSnapWords][n] (by position)
-  double *tape;      // [n][kTapeWords] (by position)
+  double *tape;      // [kTapeWords][n] (by position: a warp's lanes at the same tape
+                     // offset touch one contiguous line)
   double *alignPart; // [S][6][n] (by track)
   double *trackFs;   // [n] per-track d chi2 / d field scale (by track)
   double *chi2;      // [n]
@@ -61,16 +62,24 @@ struct AdjParams {
 
 __device__ __forceinline__ double hdr(int type, int len) { return (double)(type * 65536 + len); }
 
+// a lane's tape: word k at p[k * n]
+struct TapeRef {
+  const double *p;
+  int64_t n;
+  __device__ __forceinline__ double operator[](int k) const { return p[(int64_t)k * n]; }
+  __device__ __forceinline__ TapeRef operator+(int k) const { return {p + (int64_t)k * n, n}; }
+};
+
 struct TapeHook {
   static constexpr bool kMaterial = false;
-  double *tape;
+  double *tape; // this lane's word 0; word k at tape[k * n]
   int32_t *info;
   int64_t n;
   int top, head, state, plane;
   bool rec, full;
 
   __device__ __forceinline__ void put(double v) {
-    if (top < kTapeWords) tape[top] = v;
+    if (top < kTapeWords) tape[(int64_t)top * n] = v;
     else full = true;
     ++top;
   }
@@ -322,7 +331,7 @@ __device__ __forceinline__ void addAlign(const AdjParams &A, int64_t n, int64_t 
   kfa::alignmentGrad(f, fb, g);
   for (int a = 0; a < 6; ++a) A.alignPart[((int64_t)k * 6 + a) * n + i] += g[a];
 }
-__device__ __forceinline__ void readJT(const double *w, kfa::JT &J) {
+__device__ __forceinline__ void readJT(TapeRef w, kfa::JT &J) {
   int k = 0;
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) J.A[i][j] = w[k++];
@@ -341,14 +350,14 @@ __device__ __forceinline__ void routeStep(Adj &R, int idx, double hb) {
 // reverse of one RK step record (the uniform-field step of the fit,
 // kfa::polyAcceptFwd, and the error estimates of its rejected trials)
 // g / gp: the leg constants of momentum gp, kept across the steps of a leg
-__device__ void reverseStep(const double *w, int len, Adj &R, const Params &P, double q,
+__device__ void reverseStep(TapeRef w, int len, Adj &R, const Params &P, double q,
                             kfa::Leg &g, double &gp) {
-  const double *pos = w, *dir = w + 3;
+  const double pos[3] = {w[0], w[1], w[2]}, dir[3] = {w[3], w[4], w[5]};
   const double t = w[6], p = w[7];
   kfa::JT J0;
   readJT(w + 8, J0);
   const int T = (len - kStepFixed - 1) / 2;
-  const double *tr = w + kStepFixed;
+  const TapeRef tr = w + kStepFixed;
   if (p != gp) {
     kfa::legFwd(p, q, P.mass, g);
     gp = p;
@@ -395,7 +404,7 @@ __device__ void reverseStep(const double *w, int len, Adj &R, const Params &P, d
 
 // reverse of a navigation step-constraint update (distance to plane k from
 // the state pos, dir that the following RK step starts from)
-__device__ void reverseAct(const double *w, const double pos[3], const double dir[3], Adj &R,
+__device__ void reverseAct(TapeRef w, const double pos[3], const double dir[3], Adj &R,
                            const PlaneD *sp, const AdjParams &A, int64_t n, int64_t i) {
   if (R.ssAct == 0.) return;
   const int k = (int)w[0];
@@ -410,7 +419,7 @@ __device__ void reverseAct(const double *w, const double pos[3], const double di
 
 // reverse of a surface event with a hit: bound state (prediction, covariance
 // transport, jacToGlobal), gain update, stepper update
-__device__ void reverseHit(const double *w, Adj &R, const Params &P, const PlaneD *sp,
+__device__ void reverseHit(TapeRef w, Adj &R, const Params &P, const PlaneD *sp,
                            const AdjParams &A, int64_t u, int64_t i, double q) {
   const int64_t n = P.n;
   kfa::BoundIn in;
@@ -498,7 +507,7 @@ __device__ void reverseHit(const double *w, Adj &R, const Params &P, const Plane
 // Sweep the tapes of all lanes backwards together: step and navigation
 // records whenever a lane has one on top, surface events once every lane with
 // work has one on top.  Returns false for a malformed tape.
-__device__ bool reverseWarp(const double *tape, int top, Adj &R, const Params &P,
+__device__ bool reverseWarp(TapeRef tape, int top, Adj &R, const Params &P,
                             const PlaneD *sp, const AdjParams &A, int64_t u, int64_t i, double q) {
   bool bad = false;
   double cpos[3] = {0., 0., 0.}, cdir[3] = {0., 0., 0.}; // pre-state of the step after
@@ -517,7 +526,7 @@ __device__ bool reverseWarp(const double *tape, int top, Adj &R, const Params &P
     }
     if (__any_sync(0xffffffffu, type == REC_STEP || type == REC_ACT)) {
       if (type == REC_STEP) {
-        const double *w = tape + (top - len);
+        const TapeRef w = tape + (top - len);
         reverseStep(w, len, R, P, q, leg, legP);
         for (int e = 0; e < 3; ++e) {
           cpos[e] = w[e];
@@ -638,7 +647,7 @@ __global__ void __launch_bounds__(kLaneSlots, KF_ADJ_MIN_BLOCKS)
   const bool valid = u < P.n;
   const int64_t i = valid ? (int64_t)A.perm[u] : 0;                 // track
   ALane L;
-  L.hook.tape = A.tape + (valid ? u : 0) * kTapeWords;
+  L.hook.tape = A.tape + (valid ? u : 0);
   L.hook.info = A.info + (valid ? u : 0);
   L.hook.n = P.n;
   L.hook.top = L.hook.head = L.hook.state = L.hook.plane = 0;
@@ -679,7 +688,8 @@ __global__ void __launch_bounds__(kLaneSlots, KF_ADJ_MIN_BLOCKS)
     runWarp(L, P, sp, A, (c + 1) * kEvery, false);
     if (act && L.hook.full) failed = true;
     const bool sweep = act && !failed;
-    if (!reverseWarp(L.hook.tape, sweep ? L.hook.top : 0, R, P, sp, A, u, i, q) && sweep)
+    if (!reverseWarp(TapeRef{L.hook.tape, P.n}, sweep ? L.hook.top : 0, R, P, sp, A, u, i, q) &&
+        sweep)
       failed = true;
   }
   if (!ok) return;
