@@ -136,7 +136,12 @@ void fillParams(Params &P, const kf_inputs_t *in, const kf_outputs_t *out, const
       pl.V[r] = geo->rotation[9 * k + 3 * r + 1];
       pl.T[r] = geo->rotation[9 * k + 3 * r + 2];
     }
-    for (int e = 0; e < 6; ++e) P.planeMat[k][e] = geo->material ? geo->material[6 * k + e] : 0.;
+    {
+      double m[6] = {0., 0., 0., 0., 0., 0.};
+      if (geo->material)
+        for (int e = 0; e < 6; ++e) m[e] = geo->material[6 * k + e];
+      P.planeSlab[k] = kfm::slab(m);
+    }
   }
   P.materialEffects = (geo->material && cfg->material_effects) ? (cfg->material_effects & 3) : 0;
   P.wsCov = cfg->material_effects

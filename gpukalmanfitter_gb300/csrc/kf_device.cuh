@@ -87,7 +87,7 @@ struct Params {
   int32_t *queueCounter; // batched form: next unclaimed queue position
   FieldD field;
   PlaneD planes[KF_MAX_PLANES];
-  double planeMat[KF_MAX_PLANES][6]; // surface material (kf_geometry_t.material)
+  kfm::Slab planeSlab[KF_MAX_PLANES]; // surface material (kf_geometry_t.material)
 };
 
 // upper-triangle index of (i, j), i <= j, row-major
@@ -1096,7 +1096,7 @@ __device__ __forceinline__ double *wsCovPtr(const Params &P, const Lane<R, H> &L
 // the material interaction at plane k (material kernels only)
 static __device__ __forceinline__ bool materialStep(const Params &P, int k, const double dir[3], double p,
                                           double q, kfm::Effects &fx) {
-  return kfm::interact(P.planeMat[k], P.materialEffects, P.planes[k].T, dir, p, q, P.mass, fx);
+  return kfm::interact(P.planeSlab[k], P.materialEffects, P.planes[k].T, dir, p, q, P.mass, fx);
 }
 
 template <typename R, typename H>
@@ -1478,12 +1478,19 @@ static __device__ __forceinline__ bool smoothNoise(const Params &P, int64_t u, i
     double G[6][6];
 #pragma unroll
     for (int r = 0; r < 6; ++r) {
+      // (C_f J^T)(r, c) on J's structure: row 4 is e4, column 5 is e5 (the
+      // terms left out are exact zeros)
       double a[6];
 #pragma unroll
       for (int c = 0; c < 6; ++c) {
+        if (c == 4) {
+          a[4] = Cf[sidx(r, 4)];
+          continue;
+        }
         double v = 0.;
 #pragma unroll
-        for (int k = 0; k < 6; ++k) v += Cf[sidx(r, k)] * J[c][k];
+        for (int k = 0; k < 5; ++k) v += Cf[sidx(r, k)] * J[c][k];
+        if (c == 5) v += Cf[sidx(r, 5)];
         a[c] = v;
       }
 #pragma unroll
