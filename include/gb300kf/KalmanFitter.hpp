@@ -12,6 +12,8 @@
 //   BoundParameters           include/EventData/SingleBoundTrackParameters.hpp:27-105
 //   PlaneSurface(center, normal)  include/Surfaces/detail/PlaneSurface.ipp:24-46
 //   LineSurface(point)        include/Surfaces/detail/LineSurface.ipp:19-21
+//   InterpolatedBFieldMap from a text map, as Options::readBField reads it
+//                             src/Plugins/BFieldOptions.cpp:33-61
 //
 // The reference fits one track per call.  fit() here does the same (a batch
 // of one, convenient but slow); fitBatch() fits many tracks in one GPU launch
@@ -28,11 +30,13 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
 
 #include "../gb300kf.h"
+#include "../gb300kf_fieldmap.h"
 
 namespace gb300kf {
 
@@ -195,6 +199,42 @@ struct ConstantBField {
   Vector3D value{0., 0., 2. * kTesla};
 };
 
+/// Field map (MagneticField/InterpolatedBFieldMap.hpp, trilinear on an
+/// equidistant 3D grid) read from a text file of "x y z bx by bz" lines as
+/// Options::readBField reads the driver's map (src/Plugins/BFieldOptions.cpp:
+/// 33-61: lengths in mm, field in tesla); the grid is copied to the current
+/// device and shared by the copies of this object.  `scale` multiplies
+/// every lookup (InterpolatedBFieldMap::Config::scale).
+class InterpolatedBFieldMap {
+public:
+  explicit InterpolatedBFieldMap(const std::string &xyzFile, double lengthUnit = 1.,
+                                 double bFieldUnit = kTesla, bool firstOctant = false,
+                                 double scale = 1.) {
+    float *host = nullptr;
+    if (kf_field_map_read_xyz(xyzFile.c_str(), lengthUnit, bFieldUnit, firstOctant ? 1 : 0,
+                              &m_field, &host) != 0)
+      throw std::runtime_error(std::string("field map: ") + kf_last_error_string());
+    const size_t bytes = (size_t)m_field.nx * m_field.ny * m_field.nz * 4 * sizeof(float);
+    void *dev = nullptr;
+    const bool ok = cudaMalloc(&dev, bytes) == cudaSuccess &&
+                    cudaMemcpy(dev, host, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
+    kf_field_map_free(host);
+    if (!ok) {
+      if (dev) cudaFree(dev);
+      throw std::runtime_error("field map: device copy failed");
+    }
+    m_grid = std::shared_ptr<void>(dev, [](void *q) { cudaFree(q); });
+    m_field.grid = static_cast<const float *>(dev);
+    m_field.scale = scale;
+  }
+  /// the grid as the C ABI takes it (device memory)
+  const kf_field_t &field() const { return m_field; }
+
+private:
+  kf_field_t m_field{};
+  std::shared_ptr<void> m_grid;
+};
+
 /// One track's inputs for fitBatch.
 struct TrackInput {
   std::vector<PixelSourceLink> sourcelinks;
@@ -205,7 +245,14 @@ class KalmanFitter {
 public:
   explicit KalmanFitter(ConstantBField field = ConstantBField(),
                         PropagatorOptions options = PropagatorOptions())
-      : m_field(field), m_options(options) {}
+      : m_options(options) {
+    m_field.kind = KF_FIELD_CONSTANT;
+    m_field.scale = 1.;
+    for (int a = 0; a < 3; ++a) m_field.value[a] = field.value[a];
+  }
+  explicit KalmanFitter(const InterpolatedBFieldMap &map,
+                        PropagatorOptions options = PropagatorOptions())
+      : m_field(map.field()), m_map{map}, m_options(options) {}
   KalmanFitter(const KalmanFitter &) = delete;
   KalmanFitter &operator=(const KalmanFitter &) = delete;
   ~KalmanFitter() {
@@ -312,10 +359,7 @@ public:
     if (anyMaterial)
       cfg.material_effects = (kfOptions.multipleScattering ? 1 : 0) | (kfOptions.energyLoss ? 2 : 0);
     kf_geometry_t geo{S, 0, center.data(), rot.data(), anyMaterial ? mat.data() : nullptr};
-    kf_field_t field{};
-    field.kind = KF_FIELD_CONSTANT;
-    field.scale = 1.;
-    for (int a = 0; a < 3; ++a) field.value[a] = m_field.value[a];
+    const kf_field_t field = m_field;
     const size_t need = kf_host_staging_size(&cfg, n, S, 1);
     if (need > m_stagingBytes) {
       if (m_staging) cudaFree(m_staging);
@@ -362,7 +406,8 @@ public:
   }
 
 private:
-  ConstantBField m_field;
+  kf_field_t m_field{};
+  std::vector<InterpolatedBFieldMap> m_map; // keeps a map's device grid alive
   PropagatorOptions m_options;
   void *m_staging = nullptr;
   size_t m_stagingBytes = 0;

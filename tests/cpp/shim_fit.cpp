@@ -2,6 +2,8 @@
 // (include/gb300kf/KalmanFitter.hpp) written in the reference fitter's call
 // shape, and checks it against a direct kf_fit_batch_host call.
 #include <cstdio>
+#include <cstdlib>
+#include <string>
 #include <vector>
 
 #include "../../include/gb300kf/KalmanFitter.hpp"
@@ -74,7 +76,7 @@ int main() {
   out.chi2 = oChi.data();
   out.status = oSt.data();
   out.n_meas = oNm.data();
-  kf_geometry_t geo{S, 0, center.data(), rot.data()};
+  kf_geometry_t geo{S, 0, center.data(), rot.data(), nullptr};
   kf_field_t field{};
   field.kind = KF_FIELD_CONSTANT;
   field.scale = 1.;
@@ -140,6 +142,53 @@ int main() {
     }
   }
   if (changed < n) ++bad; // the material must change the fits
+
+  // a field map file ("x y z bx by bz" in mm and tesla, the driver's format):
+  // the shim's InterpolatedBFieldMap against the C ABI reader and a direct call
+  const char *tmp = std::getenv("TMPDIR");
+  const std::string path = std::string(tmp ? tmp : "/tmp") + "/gb300kf_shim_map.txt";
+  {
+    FILE *f = std::fopen(path.c_str(), "w");
+    if (!f) return 5;
+    std::fprintf(f, "%% x y z bx by bz\n");
+    for (int ix = 0; ix < 27; ++ix)
+      for (int iy = 0; iy < 13; ++iy)
+        for (int iz = 0; iz < 13; ++iz) {
+          const double x = -100. + 50. * ix, y = -300. + 50. * iy, z = -300. + 50. * iz;
+          std::fprintf(f, "%.17g %.17g %.17g %.17g %.17g %.17g\n", x, y, z, 1e-5 * z,
+                       -1e-5 * y, 2.0 * (1. - 2e-5 * x));
+        }
+    std::fclose(f);
+  }
+  InterpolatedBFieldMap map(path);
+  KalmanFitter mfitter(map, popt);
+  std::vector<KalmanFitterResult> fres;
+  mfitter.fitBatch(tracks, opt, fres, planes.data(), planes.size());
+  kf_field_t mf;
+  float *hgrid = nullptr;
+  if (kf_field_map_read_xyz(path.c_str(), 1., kTesla, 0, &mf, &hgrid) != 0) return 6;
+  const size_t gbytes = (size_t)mf.nx * mf.ny * mf.nz * 4 * sizeof(float);
+  void *dgrid = nullptr;
+  if (cudaMalloc(&dgrid, gbytes) != cudaSuccess) return 2;
+  cudaMemcpy(dgrid, hgrid, gbytes, cudaMemcpyHostToDevice);
+  kf_field_map_free(hgrid);
+  mf.grid = static_cast<const float *>(dgrid);
+  const size_t fbytes = kf_host_staging_size(&cfg, n, S, 0);
+  if (cudaMalloc(&dev, fbytes) != cudaSuccess) return 2;
+  if (kf_fit_batch_host(&in, &out, &cfg, &geo, &mf, dev, fbytes, nullptr) != 0) return 7;
+  cudaFree(dev);
+  cudaFree(dgrid);
+  std::remove(path.c_str());
+  int fitted = 0, moved = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    if (fres[i].status != oSt[i] || fres[i].chi2 != oChi[i]) ++bad;
+    fitted += fres[i].result ? 1 : 0;
+    for (int e = 0; e < 6; ++e) {
+      if (fres[i].fittedParameters.parameters()[e] != oPar[e * n + i]) ++bad;
+      if (fres[i].fittedParameters.parameters()[e] != res[i].fittedParameters.parameters()[e]) ++moved;
+    }
+  }
+  if (fitted < n * 9 / 10 || moved < n) ++bad; // the map fits, and differently from 2 T
   std::printf("shim tracks=%lld mismatches=%d\n", (long long)n, bad);
   return bad == 0 ? 0 : 1;
 }
