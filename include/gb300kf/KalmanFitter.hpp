@@ -26,6 +26,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <array>
 #include <cmath>
 #include <cstdint>
@@ -35,8 +36,11 @@
 #include <string>
 #include <vector>
 
+#include <ios>
+
 #include "../gb300kf.h"
 #include "../gb300kf_fieldmap.h"
+#include "../gb300kf_io.h"
 
 namespace gb300kf {
 
@@ -154,6 +158,7 @@ private:
 struct TrackState {
   BoundVector smoothed{};
   BoundSymMatrix smoothedCovariance{};
+  unsigned int surfaceIndex = 0; // position of the state's plane in the surface sequence
 };
 
 struct KalmanFitterOptions {
@@ -392,8 +397,11 @@ public:
           kfOptions.referenceSurface ? kfOptions.referenceSurface : &tracks[i].start.referenceSurface();
       r.fittedParameters = BoundParameters<LineSurface>(GeometryContext{}, C, p, target);
       r.fittedStates.resize(r.measurementStates);
+      uint64_t bits = mask[i];
       for (size_t k = 0; k < r.measurementStates; ++k) {
         TrackState &ts = r.fittedStates[k];
+        ts.surfaceIndex = bits ? (unsigned)__builtin_ctzll(bits) : (unsigned)k;
+        bits &= bits ? bits - 1 : 0;
         for (int q = 0; q < 6; ++q) ts.smoothed[q] = oSm[((size_t)k * 27 + q) * n + i];
         int f = 0;
         for (int a = 0; a < 6; ++a)
@@ -412,6 +420,56 @@ private:
   void *m_staging = nullptr;
   size_t m_stagingBytes = 0;
 };
+
+/// writeParamsCsv (Run/Common/Writer.hpp:80-110): the fitted parameters of
+/// the tracks whose status is true, one CSV row each (kf_write_params_csv).
+template <typename parameters_t>
+void writeParamsCsv(const parameters_t *params, const bool *status, unsigned int nTracks,
+                    std::string fileName) {
+  if (fileName.empty()) fileName = "params-fitted.obj"; // the reference's default name
+  std::vector<double> p((size_t)6 * nTracks);
+  std::vector<int32_t> st(nTracks);
+  for (unsigned int i = 0; i < nTracks; ++i) {
+    for (int e = 0; e < 6; ++e) p[(size_t)e * nTracks + i] = params[i].parameters()[e];
+    st[i] = status[i] ? KF_TRACK_OK : KF_TRACK_NOT_FITTED;
+  }
+  if (kf_write_params_csv(fileName.c_str(), p.data(), st.data(), nTracks, nTracks) != 0)
+    throw std::ios_base::failure(kf_last_error_string());
+}
+
+/// writeStatesObj (Run/Common/Writer.hpp:42-78) with parameters = "smoothed":
+/// one obj polyline per successful fit through its smoothed states, placed on
+/// the planes of `surfaces` (kf_write_states_obj).  Takes the fit results and
+/// the surface sequence where the reference takes its track-state array.
+inline void writeStatesObj(const KalmanFitterResult *results, unsigned int nTracks,
+                           const PlaneSurface *surfaces, unsigned int nSurfaces,
+                           std::string fileName) {
+  if (fileName.empty()) fileName = "tracks-fitted.obj";
+  if (nSurfaces == 0 || nSurfaces > KF_MAX_PLANES)
+    throw std::invalid_argument("surface sequence must hold 1..64 planes");
+  const size_t n = nTracks, S = nSurfaces;
+  std::vector<double> sm(S * 27 * n, 0.), center(3 * S), rot(9 * S);
+  std::vector<int32_t> nm(n), st(n);
+  std::vector<uint64_t> mask(n, 0);
+  for (size_t k = 0; k < S; ++k) {
+    for (int r = 0; r < 3; ++r) center[3 * k + r] = surfaces[k].center()[r];
+    for (int e = 0; e < 9; ++e) rot[9 * k + e] = surfaces[k].rotation()[e];
+  }
+  for (size_t i = 0; i < n; ++i) {
+    const KalmanFitterResult &r = results[i];
+    st[i] = r.result ? KF_TRACK_OK : KF_TRACK_NOT_FITTED;
+    nm[i] = (int32_t)std::min(r.fittedStates.size(), S);
+    for (int k = 0; k < nm[i]; ++k) {
+      const TrackState &ts = r.fittedStates[k];
+      mask[i] |= 1ull << ts.surfaceIndex;
+      for (int q = 0; q < 6; ++q) sm[((size_t)k * 27 + q) * n + i] = ts.smoothed[q];
+    }
+  }
+  const kf_geometry_t geo{(int32_t)S, 0, center.data(), rot.data(), nullptr};
+  if (kf_write_states_obj(fileName.c_str(), sm.data(), nm.data(), mask.data(), st.data(),
+                          (int64_t)n, (int64_t)n, &geo) != 0)
+    throw std::ios_base::failure(kf_last_error_string());
+}
 
 } // namespace gb300kf
 

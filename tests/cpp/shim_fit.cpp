@@ -3,6 +3,7 @@
 // shape, and checks it against a direct kf_fit_batch_host call.
 #include <cstdio>
 #include <cstdlib>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -189,6 +190,50 @@ int main() {
     }
   }
   if (fitted < n * 9 / 10 || moved < n) ++bad; // the map fits, and differently from 2 T
+
+  // the reference writers' signatures: the same CSV as the C ABI writer on the
+  // same numbers, and one obj vertex per smoothed state of a fitted track
+  {
+    const std::string csvA = std::string(tmp ? tmp : "/tmp") + "/gb300kf_shim_a.csv";
+    const std::string csvB = std::string(tmp ? tmp : "/tmp") + "/gb300kf_shim_b.csv";
+    const std::string obj = std::string(tmp ? tmp : "/tmp") + "/gb300kf_shim.obj";
+    std::vector<BoundParameters<LineSurface>> fp(n);
+    std::unique_ptr<bool[]> okv(new bool[n]);
+    size_t states = 0, lines = 0;
+    for (int64_t i = 0; i < n; ++i) {
+      fp[i] = fres[i].fittedParameters;
+      okv[i] = fres[i].result;
+      if (fres[i].result) {
+        states += fres[i].fittedStates.size();
+        lines += fres[i].fittedStates.size() - 1;
+      }
+    }
+    writeParamsCsv(fp.data(), okv.get(), (unsigned)n, csvA);
+    if (kf_write_params_csv(csvB.c_str(), oPar.data(), oSt.data(), n, n) != 0) return 8;
+    auto slurp = [](const std::string &f) {
+      std::string t;
+      FILE *h = std::fopen(f.c_str(), "rb");
+      if (!h) return t;
+      char buf[4096];
+      size_t k;
+      while ((k = std::fread(buf, 1, sizeof(buf), h)) > 0) t.append(buf, k);
+      std::fclose(h);
+      return t;
+    };
+    if (slurp(csvA).empty() || slurp(csvA) != slurp(csvB)) ++bad;
+    writeStatesObj(fres.data(), (unsigned)n, planes.data(), (unsigned)planes.size(), obj);
+    const std::string o = slurp(obj);
+    size_t nv = 0, nl = 0;
+    for (size_t k = 0; k + 1 < o.size(); ++k)
+      if (k == 0 || o[k - 1] == '\n') {
+        nv += o[k] == 'v';
+        nl += o[k] == 'l';
+      }
+    if (nv != states || nl != lines) ++bad;
+    std::remove(csvA.c_str());
+    std::remove(csvB.c_str());
+    std::remove(obj.c_str());
+  }
   std::printf("shim tracks=%lld mismatches=%d\n", (long long)n, bad);
   return bad == 0 ? 0 : 1;
 }
