@@ -1073,6 +1073,55 @@ __device__ __forceinline__ void stepperUpdate(Lane<R, H> &L, const PlaneD &pl, c
   else legConstants(L, mass);
 }
 
+// EigenStepper::update after a filter update whose predicted state is the
+// lane's current one.  The filtered angles differ from the predicted ones by
+// the gain's correction (the reference evaluates sincos of the filtered
+// angles); the predicted angles' cosines and sines are the predicted
+// direction's ratios, so the filtered ones follow from the angle-addition
+// formulas, with the correction's sine and cosine from Taylor series (|delta|
+// <= 0.02: truncation below 1e-20 absolute).  The direction is scaled by
+// sin(theta_p) before its normalisation, which removes that division.  Larger
+// corrections, and directions within 1e-6 of the z axis, take stepperUpdate.
+template <typename R, typename H>
+__device__ __forceinline__ void stepperUpdateFiltered(Lane<R, H> &L, const PlaneD &pl,
+                                                      const double pred[6], const double par[6],
+                                                      const double cov[21], double mass) {
+  const double dphi = par[2] - pred[2], dth = par[3] - pred[3];
+  const double dx = L.dir[0], dy = L.dir[1], dz = L.dir[2];
+  const double s2 = dx * dx + dy * dy;
+  if (!(fabs(dphi) <= 0.02) || !(fabs(dth) <= 0.02) || !(s2 > 1e-12)) {
+    stepperUpdate(L, pl, par, cov, mass);
+    return;
+  }
+#pragma unroll
+  for (int r = 0; r < 3; ++r) L.pos[r] = pl.U[r] * par[0] + pl.V[r] * par[1] + pl.c[r];
+  auto sinCosSmall = [](double d, double &sn, double &cs) {
+    const double d2 = d * d;
+    sn = d + d * d2 * (-1. / 6. + d2 * (1. / 120. + d2 * (-1. / 5040.)));
+    cs = 1. + d2 * (-0.5 + d2 * (1. / 24. + d2 * (-1. / 720. + d2 * (1. / 40320.))));
+  };
+  double sdp, cdp, sdt, cdt;
+  sinCosSmall(dphi, sdp, cdp);
+  sinCosSmall(dth, sdt, cdt);
+  // with s = sin(theta_p) = sqrt(s2): cos(phi_p) = dx / s, sin(phi_p) = dy / s,
+  // cos(theta_p) = dz; the direction times s
+  const double st0 = sqrt(s2);
+  const double stf = st0 * cdt + dz * sdt;   // sin(theta_f)
+  const double ctf = dz * cdt - st0 * sdt;   // cos(theta_f)
+  const double d0 = (dx * cdp - dy * sdp) * stf, d1 = (dy * cdp + dx * sdp) * stf,
+               d2 = ctf * st0;
+  const double in = rsqrt(d0 * d0 + d1 * d1 + d2 * d2);
+  L.dir[0] = d0 * in;
+  L.dir[1] = d1 * in;
+  L.dir[2] = d2 * in;
+  L.p = fabs(1. / par[4]);
+  L.t = par[5];
+#pragma unroll
+  for (int e = 0; e < 21; ++e) L.cov(e) = cov[e];
+  if constexpr (sizeof(R) == sizeof(float)) legConstantsIp(L, mass, fabs(par[4]));
+  else legConstants(L, mass);
+}
+
 // ---------------------------------------------------------------------------
 // Workspace access: state s of track i, element e
 // ---------------------------------------------------------------------------
@@ -1178,7 +1227,7 @@ __device__ void filterHit(Lane<R, H> &L, const Params &P, const PlaneD *planes, 
     if (H::kMaterial && P.materialEffects)
       for (int e = 0; e < 21; ++e) *wsCovPtr(P, L, s, 21 + e) = cf[e];
     L.chi2 += chi2;
-    stepperUpdate(L, pl, filt, cf, P.mass);
+    stepperUpdateFiltered(L, pl, pred, filt, cf, P.mass);
     if (!P.faithful) planeJacToGlobal(L, pl);
   }
   if constexpr (H::kMaterial) {
