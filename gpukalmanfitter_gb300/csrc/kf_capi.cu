@@ -195,7 +195,6 @@ void kf_config_default(kf_config_t *c) {
 }
 
 size_t kf_workspace_size(const kf_config_t *cfg, int64_t n_tracks, int32_t n_surfaces) {
-  (void)cfg;
   if (n_tracks <= 0 || n_surfaces <= 0) return 0;
   return wsBytes(n_tracks, n_surfaces, cfg && cfg->material_effects);
 }
