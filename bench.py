@@ -94,15 +94,22 @@ def env_rank():
 
 
 # ---------------------------------------------------------------------------
+_HOST_THREADS = None
+
+
 def cpu_oracle_rate(n_tracks: int, reps: int, warmup: int, seed: int,
-                    workload: str = "uniform10") -> dict:
-    """The reference algorithm on the host cores (oracle port)."""
+                    workload: str = "uniform10", threads: int = 0) -> dict:
+    """The reference algorithm on the host cores (oracle port); threads = 0:
+    all of them."""
     import gpukalmanfitter_gb300 as kf
     import oracle
     tel = make_workload(kf, workload, n_tracks, seed)
     cfg = fit_config(kf, workload, "fp64")
     lib = oracle.load()
-    threads = int(lib.oracle_num_threads())
+    global _HOST_THREADS
+    if _HOST_THREADS is None:  # before any run sets OpenMP's process-wide thread count
+        _HOST_THREADS = int(lib.oracle_num_threads())
+    threads = threads or _HOST_THREADS
     for _ in range(warmup):
         oracle.fit(tel, cfg, threads=threads)
     times = []
@@ -492,6 +499,11 @@ def run_gpu(args) -> None:
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_oracle_rate(CPU_SAMPLE, 3, 1, seed=1234567890, workload=args.workload)
         cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        # the same loop on one host thread (a tenth of the sample)
+        one = cpu_oracle_rate(max(1, CPU_SAMPLE // 10), 3, 1, seed=1234567890,
+                              workload=args.workload, threads=1)
+        cpu["single_thread"] = {"value": one["value"], "unit": UNIT, "cores": 1,
+                                "sample": one["sample"]}
 
     if rank == 0:
         line = {
