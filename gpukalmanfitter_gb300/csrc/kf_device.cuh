@@ -1196,6 +1196,7 @@ __device__ void filterHit(Lane<R, H> &L, const Params &P, const PlaneD *planes, 
 #pragma unroll
     for (int i = 0; i < 6; ++i) filt[i] = pred[i] + (K0[i] * r0 + K1[i] * r1);
     if constexpr (sizeof(R) == sizeof(double)) {
+      // the reference's C_f = (I - KH) C (GainMatrixUpdater.hpp:77-84)
 #pragma unroll
       for (int i = 0; i < 6; ++i) {
 #pragma unroll
@@ -1203,23 +1204,22 @@ __device__ void filterHit(Lane<R, H> &L, const Params &P, const PlaneD *planes, 
           cf[ut(i, j)] = L.cov(ut(i, j)) - K0[i] * L.cov(sidx(0, j)) - K1[i] * L.cov(sidx(1, j));
       }
     } else {
-      // Joseph form with H = [I2 0]:
-      //   C - K A - A^T K^T + K (S0 + V) K^T,  A = H C, S0 + V = S
-      double KS0[6], KS1[6];
+      // Joseph form with H = [I2 0], A = H C (rows 0-1 of C), S = H C H^T + V:
+      //   (I - KH) C (I - KH)^T + K V K^T = C - K A - A^T K^T + K S K^T,
+      // entry (i, j) = C_ij - K_i . A_j - K_j . (A_i - (K S)_i): four FMAs an
+      // entry once D_i = A_i - (K S)_i is formed
+      double D0[6], D1[6];
 #pragma unroll
       for (int i = 0; i < 6; ++i) {
-        KS0[i] = K0[i] * S00 + K1[i] * S10;
-        KS1[i] = K0[i] * S01 + K1[i] * S11;
+        D0[i] = L.cov(sidx(0, i)) - (K0[i] * S00 + K1[i] * S10);
+        D1[i] = L.cov(sidx(1, i)) - (K0[i] * S01 + K1[i] * S11);
       }
 #pragma unroll
       for (int i = 0; i < 6; ++i) {
 #pragma unroll
-        for (int j = i; j < 6; ++j) {
-          const double ka = K0[i] * L.cov(sidx(0, j)) + K1[i] * L.cov(sidx(1, j));
-          const double ak = K0[j] * L.cov(sidx(0, i)) + K1[j] * L.cov(sidx(1, i));
-          const double ksk = KS0[i] * K0[j] + KS1[i] * K1[j];
-          cf[ut(i, j)] = (L.cov(ut(i, j)) - ka) - (ak - ksk);
-        }
+        for (int j = i; j < 6; ++j)
+          cf[ut(i, j)] = L.cov(ut(i, j)) - K0[i] * L.cov(sidx(0, j)) - K1[i] * L.cov(sidx(1, j)) -
+                         K0[j] * D0[i] - K1[j] * D1[i];
       }
     }
 #pragma unroll
