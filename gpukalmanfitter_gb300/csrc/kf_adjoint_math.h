@@ -22,6 +22,16 @@
 
 namespace kfa {
 
+// sine and cosine of one angle (one argument reduction on the device)
+KF_HD void sinCos(double x, double &sn, double &cs) {
+#ifdef __CUDA_ARCH__
+  sincos(x, &sn, &cs);
+#else
+  sn = std::sin(x);
+  cs = std::cos(x);
+#endif
+}
+
 KF_HD void cross(const double a[3], const double b[3], double r[3]) {
   r[0] = a[1] * b[2] - a[2] * b[1];
   r[1] = a[2] * b[0] - a[0] * b[2];
@@ -1126,11 +1136,11 @@ struct FilterTmp {
 KF_HD void filterFwd(const double pred[6], const double C[21], const double mv[5],
                      double filt[6], double cf[21], double *chi2, FilterTmp &w) {
   const double S00 = C[0] + mv[2], S01 = C[1] + mv[3], S10 = C[1] + mv[3], S11 = C[6] + mv[4];
-  const double det = S00 * S11 - S01 * S10;
-  w.i00 = S11 / det;
-  w.i01 = -S01 / det;
-  w.i10 = -S10 / det;
-  w.i11 = S00 / det;
+  const double idet = 1. / (S00 * S11 - S01 * S10);
+  w.i00 = S11 * idet;
+  w.i01 = -S01 * idet;
+  w.i10 = -S10 * idet;
+  w.i11 = S00 * idet;
   w.r0 = mv[0] - pred[0];
   w.r1 = mv[1] - pred[1];
   *chi2 = w.r0 * (w.i00 * w.r0 + w.i01 * w.r1) + w.r1 * (w.i10 * w.r0 + w.i11 * w.r1);
@@ -1195,7 +1205,9 @@ KF_HD void filterVjp(const double C[21], const FilterTmp &w, const double filtb[
 KF_HD void updateFwd(const Frame &f, const double x[6], double pos[3], double d[3], double *p,
                      double *t, double trig[4] = nullptr) {
   for (int r = 0; r < 3; ++r) pos[r] = f.U[r] * x[0] + f.V[r] * x[1] + f.c[r];
-  const double sp = sin(x[2]), cp = cos(x[2]), st = sin(x[3]), ct = cos(x[3]);
+  double sp, cp, st, ct;
+  sinCos(x[2], sp, cp);
+  sinCos(x[3], st, ct);
   if (trig) {
     trig[0] = sp;
     trig[1] = cp;
@@ -1203,8 +1215,8 @@ KF_HD void updateFwd(const Frame &f, const double x[6], double pos[3], double d[
     trig[3] = ct;
   }
   const double v[3] = {cp * st, sp * st, ct};
-  const double n = sqrt(dot(v, v));
-  for (int i = 0; i < 3; ++i) d[i] = v[i] / n;
+  const double in = 1. / sqrt(dot(v, v));
+  for (int i = 0; i < 3; ++i) d[i] = v[i] * in;
   *p = fabs(1. / x[4]);
   *t = x[5];
 }
@@ -1220,10 +1232,10 @@ KF_HD void updateVjp(const Frame &f, const double x[6], const double d[3], const
     fb.c[r] += posb[r];
   }
   const double v[3] = {cp * st, sp * st, ct};
-  const double n = sqrt(dot(v, v));
+  const double in = 1. / sqrt(dot(v, v));
   const double pr = dot(d, db);
   double vb[3];
-  for (int i = 0; i < 3; ++i) vb[i] = (db[i] - d[i] * pr) / n;
+  for (int i = 0; i < 3; ++i) vb[i] = (db[i] - d[i] * pr) * in;
   xb[2] += vb[0] * (-sp * st) + vb[1] * (cp * st);
   xb[3] += vb[0] * (cp * ct) + vb[1] * (sp * ct) - vb[2] * st;
   xb[4] += pb * (-(x[4] > 0. ? 1. : -1.) / (x[4] * x[4]));
