@@ -806,20 +806,24 @@ KF_HD void dirCoefFwd(const double d[3], DirCoef &k) {
 }
 KF_HD void dirCoefVjp(const double d[3], const DirCoef &kb, double db[3]) {
   const double x = d[0], y = d[1], z = d[2];
-  const double r2 = x * x + y * y, s = sqrt(r2), s3 = r2 * s, r4 = r2 * r2;
+  // powers of 1/s, s = sqrt(x^2 + y^2), from one reciprocal
+  const double s = sqrt(x * x + y * y), is = 1. / s, ir2 = is * is, is3 = ir2 * is,
+               ir4 = ir2 * ir2;
   // j24 = -y / r2, j25 = x / r2
-  db[0] += kb.j24 * (2. * x * y / r4) + kb.j25 * ((y * y - x * x) / r4);
-  db[1] += kb.j24 * ((y * y - x * x) / r4) + kb.j25 * (-2. * x * y / r4);
+  db[0] += kb.j24 * (2. * x * y * ir4) + kb.j25 * ((y * y - x * x) * ir4);
+  db[1] += kb.j24 * ((y * y - x * x) * ir4) + kb.j25 * (-2. * x * y * ir4);
   // j34 = x z / s, j35 = y z / s, j36 = -s
-  db[0] += kb.j34 * (z * y * y / s3) + kb.j35 * (-x * y * z / s3) + kb.j36 * (-x / s);
-  db[1] += kb.j34 * (-x * y * z / s3) + kb.j35 * (z * x * x / s3) + kb.j36 * (-y / s);
-  db[2] += kb.j34 * (x / s) + kb.j35 * (y / s);
+  db[0] += kb.j34 * (z * y * y * is3) + kb.j35 * (-x * y * z * is3) + kb.j36 * (-x * is);
+  db[1] += kb.j34 * (-x * y * z * is3) + kb.j35 * (z * x * x * is3) + kb.j36 * (-y * is);
+  db[2] += kb.j34 * (x * is) + kb.j35 * (y * is);
   // g46: [[-y, x z / s], [x, y z / s], [0, -s]]
   db[1] -= kb.g46[0][0];
   db[0] += kb.g46[1][0];
-  db[0] += kb.g46[0][1] * (z * y * y / s3) + kb.g46[1][1] * (-x * y * z / s3) + kb.g46[2][1] * (-x / s);
-  db[1] += kb.g46[0][1] * (-x * y * z / s3) + kb.g46[1][1] * (z * x * x / s3) + kb.g46[2][1] * (-y / s);
-  db[2] += kb.g46[0][1] * (x / s) + kb.g46[1][1] * (y / s);
+  db[0] += kb.g46[0][1] * (z * y * y * is3) + kb.g46[1][1] * (-x * y * z * is3) +
+           kb.g46[2][1] * (-x * is);
+  db[1] += kb.g46[0][1] * (-x * y * z * is3) + kb.g46[1][1] * (z * x * x * is3) +
+           kb.g46[2][1] * (-y * is);
+  db[2] += kb.g46[0][1] * (x * is) + kb.g46[1][1] * (y * is);
 }
 
 struct BoundIn {
@@ -837,7 +841,7 @@ struct BoundOut {
 struct BoundTmp {
   double Pt0[3][5], Dd0[3][5], R30[5]; // before the derivative subtraction
   double Pt[3][5], Dd[3][5], R3[5];
-  double sVec[5], nv[3], dp, der[7];
+  double sVec[5], nv[3], dp, idp, der[7];
   double Jf[6][6], M[6][6];
   DirCoef k;
 };
@@ -864,7 +868,8 @@ KF_HD void boundFwd(const BoundIn &in, const Frame &f, BoundOut &o, BoundTmp &w,
   for (int c = 0; c < 4; ++c) w.R30[c] = 0.;
   w.R30[4] = in.J.b;
   w.dp = dot(f.T, in.dir);
-  for (int i = 0; i < 3; ++i) w.nv[i] = f.T[i] / w.dp;
+  w.idp = 1. / w.dp;
+  for (int i = 0; i < 3; ++i) w.nv[i] = f.T[i] * w.idp;
   for (int c = 0; c < 5; ++c)
     w.sVec[c] = w.nv[0] * w.Pt0[0][c] + w.nv[1] * w.Pt0[1][c] + w.nv[2] * w.Pt0[2][c];
   for (int r = 0; r < 3; ++r) {
@@ -980,17 +985,17 @@ KF_HD void boundVjp(const BoundIn &in, const Frame &f, const BoundOut &o, const 
   {
     const double x = in.dir[0], y = in.dir[1], z = in.dir[2];
     const double r2 = x * x + y * y, s = sqrt(r2), rho2 = r2 + z * z;
+    const double is = 1. / s, ir2 = is * is, irho2 = 1. / rho2;
     // phi = atan2(y, x), theta = atan2(s, z) (scale-free in the momentum)
-    ib.dir[0] += ob.pred[2] * (-y / r2);
-    ib.dir[1] += ob.pred[2] * (x / r2);
-    const double sb = ob.pred[3] * (z / rho2);
-    ib.dir[2] += ob.pred[3] * (-s / rho2);
-    ib.dir[0] += sb * x / s;
-    ib.dir[1] += sb * y / s;
-    // q/p = charge / (p |d|)
-    const double dn2 = rho2;
+    ib.dir[0] += ob.pred[2] * (-y * ir2);
+    ib.dir[1] += ob.pred[2] * (x * ir2);
+    const double sb = ob.pred[3] * (z * irho2);
+    ib.dir[2] += ob.pred[3] * (-s * irho2);
+    ib.dir[0] += sb * x * is;
+    ib.dir[1] += sb * y * is;
+    // q/p = charge / (p |d|), |d|^2 = rho2
     ib.p += ob.pred[4] * (-o.pred[4] / in.p);
-    for (int i = 0; i < 3; ++i) ib.dir[i] += ob.pred[4] * (-o.pred[4] * in.dir[i] / dn2);
+    for (int i = 0; i < 3; ++i) ib.dir[i] += ob.pred[4] * (-o.pred[4] * in.dir[i] * irho2);
   }
   ib.t += ob.pred[5];
   // ---- new jacToGlobal
@@ -1101,9 +1106,9 @@ KF_HD void boundVjp(const BoundIn &in, const Frame &f, const BoundOut &o, const 
       Ptb[r][c] += sVb[c] * w.nv[r];
     }
   {
-    const double dpb = -dot(nvb, f.T) / (w.dp * w.dp);
+    const double dpb = -dot(nvb, f.T) * (w.idp * w.idp);
     for (int i = 0; i < 3; ++i) {
-      fb.T[i] += nvb[i] / w.dp + dpb * in.dir[i];
+      fb.T[i] += nvb[i] * w.idp + dpb * in.dir[i];
       ib.dir[i] += dpb * f.T[i];
     }
   }
@@ -1252,10 +1257,11 @@ KF_HD void legFwd(double p, double q, double mass, Leg &g) {
 }
 KF_HD void legVjp(double p, double q, double mass, const Leg &g, double qopb, double dtdsb,
                   double d37b, double &pb) {
-  const double ddt = -(mass * mass) / (p * p * p) / g.dtds;
-  pb += qopb * (-q / (p * p));
+  const double ip = 1. / p, idt = 1. / g.dtds;
+  const double ddt = -(mass * mass) * (ip * ip * ip) * idt;
+  pb += qopb * (-q * (ip * ip));
   pb += dtdsb * ddt;
-  pb += d37b * (-g.d37 / p - g.d37 / g.dtds * ddt);
+  pb += d37b * (-g.d37 * ip - g.d37 * idt * ddt);
 }
 
 // ---------------------------------------------------------------------------
