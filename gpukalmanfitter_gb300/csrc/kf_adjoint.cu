@@ -581,7 +581,8 @@ __device__ double smoothChi2(const Params &P, const AdjParams &A, int64_t u, int
     const double v00 = mp[2 * P.stride], v01 = mp[3 * P.stride], v11 = mp[4 * P.stride];
     const double r0 = mp[0] - XS(s, 0), r1 = mp[P.stride] - XS(s, 1);
     const double det = v00 * v11 - v01 * v01;
-    const double w0 = (v11 * r0 - v01 * r1) / det, w1 = (v00 * r1 - v01 * r0) / det;
+    const double idet = 1. / det;
+    const double w0 = (v11 * r0 - v01 * r1) * idet, w1 = (v00 * r1 - v01 * r0) * idet;
     chi2 += r0 * w0 + r1 * w1;
     g[0] = -2. * w0;
     g[1] = -2. * w1;

@@ -1251,9 +1251,10 @@ struct Leg {
   double qop, dtds, d37;
 };
 KF_HD void legFwd(double p, double q, double mass, Leg &g) {
-  g.qop = q / p;
-  g.dtds = hypot(1., mass / p);
-  g.d37 = mass * mass * q / (p * g.dtds);
+  const double ip = 1. / p;
+  g.qop = q * ip;
+  g.dtds = hypot(1., mass * ip);
+  g.d37 = mass * mass * q * ip / g.dtds;
 }
 KF_HD void legVjp(double p, double q, double mass, const Leg &g, double qopb, double dtdsb,
                   double d37b, double &pb) {
