@@ -732,9 +732,10 @@ KF_HD double pathFwd(const double pos[3], const double d[3], const double c[3],
 }
 KF_HD void pathVjp(const double pos[3], const double d[3], const double c[3], const double T[3],
                    double pb, double posb[3], double db[3], double cb[3], double Tb[3]) {
-  const double den = dot(d, T);
-  const double path = pathFwd(pos, d, c, T);
-  const double g = pb / den;
+  const double iden = 1. / dot(d, T);
+  const double path = (T[0] * (c[0] - pos[0]) + T[1] * (c[1] - pos[1]) + T[2] * (c[2] - pos[2])) *
+                      iden;
+  const double g = pb * iden;
   for (int i = 0; i < 3; ++i) {
     posb[i] -= T[i] * g;
     cb[i] += T[i] * g;
