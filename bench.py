@@ -22,9 +22,13 @@ production: 4M uneven tracks simulated on the GPU against the host generator.
                   [--form batched|plain] [--workload W] [--precision fp64|mixed]
                   [--tracks N] [--no-suite] [--no-e2e] [--no-cpu-baseline]
 
-The reference arm times the reference algorithm's CPU path (the C++ FP64
-restatement in oracle/, OpenMP over all host cores, the reference's -d cpu
-loop shape) on a bounded sample of the same workload.
+The reference arm (--impl reference) times the reference algorithm's CPU
+path (the C++ FP64 restatement in oracle/, OpenMP over all host cores, the
+reference's -d cpu loop shape) on the same workload, config and track count
+as the GPU arm; its inputs come from the oracle library's copy of the host
+generator, so that arm never loads the product library.  With --gpus N the
+GPU arm splits one global batch of N x tracks over the ranks
+(gpukalmanfitter_gb300.shard); the reference arm runs on rank 0 alone.
 """
 from __future__ import annotations
 
@@ -47,7 +51,8 @@ sys.path.insert(0, str(ROOT))
 METRIC = "fitted tracks/s on 1 GB300, plain vs batched form at equal accuracy; grads/s"
 UNIT = "tracks/s"
 OVERSTEP = 0.1  # mm; the reference's fixed 0.01 mm skips planes on this workload
-CPU_SAMPLE = 100_000
+SINGLE_THREAD_SAMPLE = 20_000  # tracks of the one-thread CPU leg (about 0.4 s a step)
+DATA = "synthetic (seeded generator, analytic-helix truth)"
 
 # workload name -> (description, make_telescope keyword arguments, fit config extras)
 WORKLOADS = {
@@ -79,8 +84,11 @@ def workload_config(name: str, n_tracks: int, precision: str) -> dict:
             "l2": "inputs larger than the 129 MB L2 at 1M tracks"}
 
 
-def make_workload(kf, name: str, n: int, seed: int):
-    return kf.make_telescope(n, seed=seed, **WORKLOADS[name][1])
+def make_workload(kf, name: str, n: int, seed: int, lib=None):
+    """The named workload (host arrays).  lib: the library whose host
+    generator makes it (the oracle's for the reference arm, so that arm never
+    maps the product library; both carry the same generator code)."""
+    return kf.make_telescope(n, seed=seed, lib=lib, **WORKLOADS[name][1])
 
 
 def fit_config(kf, name: str, precision: str):
@@ -94,49 +102,53 @@ def env_rank():
 
 
 # ---------------------------------------------------------------------------
-_HOST_THREADS = None
-
-
-def cpu_oracle_rate(n_tracks: int, reps: int, warmup: int, seed: int,
-                    workload: str = "uniform10", threads: int = 0) -> dict:
-    """The reference algorithm on the host cores (oracle port); threads = 0:
-    all of them."""
-    import gpukalmanfitter_gb300 as kf
+def cpu_oracle_rate(tel, cfg, reps: int, warmup: int, threads: int = 0) -> dict:
+    """The reference algorithm's CPU path (the oracle, OpenMP over the track
+    loop as the reference's -d cpu driver runs it) on the tracks of `tel`:
+    wall clock around the track loop alone, median over `reps` steps.
+    threads = 0: every host thread OpenMP offers."""
     import oracle
-    tel = make_workload(kf, workload, n_tracks, seed)
-    cfg = fit_config(kf, workload, "fp64")
-    lib = oracle.load()
-    global _HOST_THREADS
-    if _HOST_THREADS is None:  # before any run sets OpenMP's process-wide thread count
-        _HOST_THREADS = int(lib.oracle_num_threads())
-    threads = threads or _HOST_THREADS
+    fitter = oracle.Fitter(tel, cfg)
+    threads = threads or int(fitter.lib.oracle_num_threads())
     for _ in range(warmup):
-        oracle.fit(tel, cfg, threads=threads)
+        fitter.run(threads)
     times = []
     for _ in range(reps):
         t0 = time.perf_counter()
-        oracle.fit(tel, cfg, threads=threads)
+        fitter.run(threads)
         times.append(time.perf_counter() - t0)
     med = statistics.median(times)
-    return {"value": n_tracks / med, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{n_tracks} tracks of the same workload per step, median of {reps} timed steps "
-                      f"({warmup} warm-up), std::chrono-style wall clock around the OpenMP track loop",
-            "seconds_per_step": med}
+    ok = float(np.mean(fitter.out["status"] == 0))
+    return {"value": tel.n / med, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"all {tel.n} tracks of the workload per step, median of {reps} timed steps "
+                      f"({warmup} warm-up), wall clock around the OpenMP track loop",
+            "seconds_per_step": med, "seconds": times, "fitted_fraction": ok}
 
 
 def run_reference(args) -> None:
+    """The reference arm: the reference algorithm's CPU path on the host
+    cores, on the GPU arm's workload, config and track count.  Inputs come
+    from the oracle library's copy of the host generator and the fit from the
+    oracle: the product library is never loaded here."""
     rank, world, _ = env_rank()
     if rank != 0:
         return
-    base = cpu_oracle_rate(CPU_SAMPLE, args.steps, args.warmup, seed=1234567890,
-                           workload=args.workload)
+    import gpukalmanfitter_gb300 as kf  # Python helpers only (structs, array layout)
+    import oracle
+    lib = oracle.load()
+    tel = make_workload(kf, args.workload, args.tracks, 1234567890, lib=lib)
+    cfg = oracle.default_config(overstep_limit=OVERSTEP, **WORKLOADS[args.workload][2])
+    base = cpu_oracle_rate(tel, cfg, args.steps, args.warmup)
+    ms = base["seconds_per_step"] * 1e3
     line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": UNIT,
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": base["seconds_per_step"] * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {**workload_config(args.workload, CPU_SAMPLE, "fp64"),
-                       "note": "reference algorithm restated in C++ FP64 (oracle/kf_oracle.cpp); "
-                               "the reference binary needs Eigen3/Boost/ROOT, absent here"},
+            "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
+            "config": workload_config(args.workload, args.tracks, "fp64"),
+            "reference_path": "the reference algorithm's -d cpu path restated in C++ FP64 "
+                              "(oracle/kf_oracle.cpp, OpenMP track loop); the reference binary "
+                              "needs Eigen3, Boost and ROOT, absent here",
+            "fitted_fraction": base["fitted_fraction"],
             "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -400,6 +412,58 @@ def output_entry(kf, n: int, seed: int, stream) -> dict:
     return out
 
 
+def rank_workload(kf, name: str, n: int, rank: int, world: int, seed: int):
+    """This rank's share of one global batch of world * n tracks.  One GPU:
+    the host generator's n tracks (the reference arm's inputs exactly).
+    Several: every rank simulates the global batch on its own GPU
+    (kf_simulate_tracks, the host generator's tracks) and keeps the tracks
+    shard.rank_tracks deals it (warp-sized chunks of the work-key order,
+    round-robin), as host arrays."""
+    if world == 1:
+        return make_workload(kf, name, n, seed)
+    import torch
+    from gpukalmanfitter_gb300 import shard
+    glob = kf.make_telescope(world * n, seed=seed, device="cuda", **WORKLOADS[name][1])
+    torch.cuda.synchronize()
+    mine = shard.subset(glob, shard.rank_tracks(glob, rank, world)).to_host()
+    if mine.field_grid is not None and hasattr(mine.field_grid, "cpu"):
+        mine.field_grid = mine.field_grid.cpu().numpy()
+    del glob
+    torch.cuda.empty_cache()
+    return mine
+
+
+def suite_summary(suite: dict | None, e2e: dict | None, ref_cpu: dict | None) -> dict:
+    """The suite's times and ratios in a few hundred bytes, printed as the
+    line's last key."""
+    out = {}
+    r = lambda v, d=3: None if v is None else round(float(v), d)
+    if suite:
+        b = suite.get("batching")
+        if b:
+            out["batching_4M_holes30_ms"] = {"plain_fp64": r(b["plain_fp64_ms_per_step"], 1),
+                                             "batched_fp64": r(b["batched_fp64_ms_per_step"], 1),
+                                             "batched_mixed": r(b["batched_mixed_ms_per_step"], 1)}
+            out["batched_fp64_over_plain"] = r(b["batched_fp64_vs_plain_fp64"])
+        m = suite.get("precision_map")
+        if m:
+            out["map30_1M_ms"] = {"plain_fp64": r(m["plain_fp64_ms_per_step"], 1),
+                                  "batched_fp64": r(m["batched_fp64_ms_per_step"], 1),
+                                  "batched_mixed": r(m["batched_mixed_ms_per_step"], 1)}
+            out["mixed_over_plain_fp64"] = r(m["batched_mixed_vs_plain_fp64"])
+            out["mixed_over_batched_fp64"] = r(m["batched_fp64_ms_per_step"] /
+                                               m["batched_mixed_ms_per_step"])
+        d = suite.get("differentiation")
+        if d:
+            out["adjoint_256k_ms"] = {"adjoint": r(d["adjoint_ms"], 1),
+                                      "fit_plain_fp64": r(d["fit_plain_fp64_ms"], 1)}
+            out["adjoint_over_plain_fit"] = r(d["adjoint_over_plain_fit"])
+            out["grads_per_s"] = r(d["tracks_differentiated_per_s"], 0)
+    if e2e and ref_cpu:
+        out["e2e_over_cpu_baseline"] = r(e2e["value"] / ref_cpu["value"], 2)
+    return out
+
+
 def run_gpu(args) -> None:
     import torch
     import gpukalmanfitter_gb300 as kf
@@ -411,8 +475,8 @@ def run_gpu(args) -> None:
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    n = args.tracks
-    tel = make_workload(kf, args.workload, n, 1234567890 + rank)
+    tel = rank_workload(kf, args.workload, args.tracks, rank, world, 1234567890)
+    n = tel.n  # this rank's tracks (args.tracks, up to a warp chunk when sharded)
     cfg = fit_config(kf, args.workload, args.precision)
     lib = kf.load()
 
@@ -421,6 +485,14 @@ def run_gpu(args) -> None:
             dist.barrier()
         torch.cuda.synchronize()
 
+    def total(count: int) -> int:
+        if dist is None:
+            return count
+        t = torch.tensor([count], dtype=torch.int64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        return int(t.item())
+
+    n_total = total(n)
     stream = torch.cuda.Stream()
     with torch.cuda.stream(stream):
         batch = kf.DeviceBatch(tel, cfg)
@@ -440,14 +512,18 @@ def run_gpu(args) -> None:
         t = torch.tensor([elapsed_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         elapsed_ms = float(t.item())
-    value = n * args.steps * world / (elapsed_ms * 1e-3)
+    value = n_total * args.steps / (elapsed_ms * 1e-3)
     res = batch.results()
 
     # the other form on the same batch (same precision): plain vs batched
     forms = {args.form: value}
     if args.form == "batched":
         pms, _ = timed_steps(lambda: batch.fit(stream), stream, args.steps, args.warmup, barrier)
-        forms["plain"] = n * args.steps * world / (pms * 1e-3)
+        if dist is not None:
+            t = torch.tensor([pms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            pms = float(t.item())
+        forms["plain"] = n_total * args.steps / (pms * 1e-3)
         forms["max_param_diff_over_scale"] = param_diff(batch.results(), res)
     batch.destroy_plan()
 
@@ -471,7 +547,7 @@ def run_gpu(args) -> None:
         if args.form == "batched":
             ecfg.kernel, ecfg.block_size = 2, shape["threads_per_cta"]
             ecfg.min_blocks_per_sm = shape["ctas_per_sm"]
-        e2e = run_e2e(kf, lib, tel, ecfg, stream, args, barrier, dist)
+        e2e = run_e2e(kf, lib, tel, ecfg, stream, args, barrier, dist, n_total)
     del batch
     torch.cuda.empty_cache()
 
@@ -497,11 +573,14 @@ def run_gpu(args) -> None:
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_oracle_rate(CPU_SAMPLE, 3, 1, seed=1234567890, workload=args.workload)
-        cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
-        # the same loop on one host thread (a tenth of the sample)
-        one = cpu_oracle_rate(max(1, CPU_SAMPLE // 10), 3, 1, seed=1234567890,
-                              workload=args.workload, threads=1)
+        # the reference algorithm's CPU path on this run's own tracks, all host
+        # threads, then one host thread on the first SINGLE_THREAD_SAMPLE tracks
+        import oracle
+        ocfg = oracle.default_config(overstep_limit=OVERSTEP, **WORKLOADS[args.workload][2])
+        base = cpu_oracle_rate(tel, ocfg, 3, 1)
+        cpu = {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        one = cpu_oracle_rate(make_workload(kf, args.workload, min(n, SINGLE_THREAD_SAMPLE),
+                                            1234567890), ocfg, 3, 1, threads=1)
         cpu["single_thread"] = {"value": one["value"], "unit": UNIT, "cores": 1,
                                 "sample": one["sample"]}
 
@@ -511,10 +590,11 @@ def run_gpu(args) -> None:
             "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if args.precision == "fp64" else "f32+f64",
-            "data": "synthetic (seeded generator, analytic-helix truth)",
-            "config": {**workload_config(args.workload, n, args.precision),
-                       "form": args.form, "kernel_shape": shape,
-                       "parallelism": f"track shards, {world} GPU(s), no collective"},
+            "data": DATA,
+            "config": workload_config(args.workload, args.tracks, args.precision),
+            "form": {"form": args.form, "kernel_shape": shape,
+                     "parallelism": f"one global batch of {n_total} tracks in balanced shards "
+                                    f"over {world} GPU(s), no collective on the fit"},
             "forms": forms,
             "fitted_fraction": ok_frac,
             "gpu_launches": args.steps * per_step,
@@ -522,9 +602,9 @@ def run_gpu(args) -> None:
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak_tflops,
                          "unit": "TFLOP/s", "frac": (achieved / peak_tflops) if peak_tflops else None,
                          "traffic": traffic,
-                         "peak_source": "measured in this run by kf_diag_fp64_fma_rate (independent "
-                                        "DFMA chains on all SMs); MEASURED_PEAKS.json is absent and "
-                                        "lists no FP64 peak",
+                         "peak_source": "FP64 DFMA rate measured in this run by kf_diag_fp64_fma_rate "
+                                        "(independent DFMA chains on all SMs): MEASURED_PEAKS.json "
+                                        "has no FP64 entry (HBM and bf16 only)",
                          "algorithmic_flop_per_launch": flop,
                          "algorithmic_flop_per_track": flop / n,
                          "dense_reference_flop_per_track": dense_flop / n,
@@ -541,6 +621,7 @@ def run_gpu(args) -> None:
             line["suite"] = suite
         if cpu is not None:
             line["cpu_baseline"] = cpu
+        line["suite_summary"] = suite_summary(suite, e2e, cpu)
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
@@ -571,10 +652,10 @@ def hbm_peak_gbs() -> tuple:
                 return float(v), "MEASURED_PEAKS.json hbm_gbs (measured)"
         except ValueError:
             pass
-    return 6800.0, "fallback 6.8 TB/s (MEASURED_PEAKS.json absent)"
+    return 6800.0, "fallback 6.8 TB/s (no hbm_gbs in MEASURED_PEAKS.json)"
 
 
-def run_e2e(kf, lib, tel, cfg, stream, args, barrier, dist) -> dict:
+def run_e2e(kf, lib, tel, cfg, stream, args, barrier, dist, n_total: int) -> dict:
     import torch
     n, S = tel.n, tel.n_surfaces
 
@@ -623,10 +704,9 @@ def run_e2e(kf, lib, tel, cfg, stream, args, barrier, dist) -> dict:
         t = torch.tensor([dt], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         dt = float(t.item())
-    world = dist.get_world_size() if dist is not None else 1
     h2d = sum(v.nbytes for v in host_in.values() if v is not None)
     d2h = sum(host_out[k].nbytes for k in ("params", "cov", "chi2", "status", "n_meas", "n_steps", "n_trials"))
-    return {"value": n * args.steps * world / dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+    return {"value": n_total * args.steps / dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
             "d2h_bytes_per_step": int(d2h),
             "path": "kf_fit_batch_host: pinned host SoA -> device staging -> fit -> host, synchronised per step"}
 

@@ -268,9 +268,9 @@ def silicon(thickness_mm: float) -> np.ndarray:
     return np.array([thickness_mm, 93.70, 465.2, 28.0855, 14.0, (2.329 / 28.0855) / 1000.0])
 
 
-def synth_config(**kw) -> SynthConfig:
+def synth_config(lib=None, **kw) -> SynthConfig:
     c = SynthConfig()
-    load().kf_synth_config_default(C.byref(c))
+    (lib or load()).kf_synth_config_default(C.byref(c))
     for k, v in kw.items():
         setattr(c, k, v)
     return c
@@ -282,7 +282,7 @@ def make_telescope(n: int, *, seed: int = 1234567890, n_planes: int = 10,
                    outlier_prob: float = 0.0, field_map=False, field_n: int = 101,
                    field_half: float = 1500.0, mis_shift: float = 0.0, mis_rot: float = 0.0,
                    material: float = 0.0, threads: int = 0, device: str | None = None,
-                   **extra) -> Telescope:
+                   lib=None, **extra) -> Telescope:
     """Seeded synthetic telescope workload (host arrays).  material > 0: every
     plane carries that many mm of silicon (the reference driver's 0.5 mm,
     Run/GPU/KalmanFitterGPUTest.cu:253) in the geometry and in the truth.
@@ -291,9 +291,14 @@ def make_telescope(n: int, *, seed: int = 1234567890, n_planes: int = 10,
     file; the truth and the fit then use that grid.  device ("cuda", ...):
     the tracks are simulated on that GPU (kf_simulate_tracks, the same
     tracks as the host generator's) and the per-track arrays are torch
-    tensors there (Telescope.to_host() gives the numpy form)."""
-    lib = load()
-    cfg = synth_config(n_tracks=n, seed=seed, n_planes=n_planes, x_first=x_first, x_step=x_step,
+    tensors there (Telescope.to_host() gives the numpy form).  lib: another
+    library exporting the host generator's kf_synth_* entry points (the
+    oracle's, which carries the same host code), in place of this one's; host
+    generation only."""
+    if lib is not None and device is not None:
+        raise KfError("make_telescope: lib= generates on the host; device= needs libgb300kf")
+    lib = lib or load()
+    cfg = synth_config(lib, n_tracks=n, seed=seed, n_planes=n_planes, x_first=x_first, x_step=x_step,
                        min_len=min_len or n_planes, max_len=max_len or n_planes,
                        hit_prob=hit_prob, outlier_prob=outlier_prob,
                        mis_shift_sigma=mis_shift, mis_rot_sigma=mis_rot, **extra)

@@ -780,6 +780,7 @@ int32_t kf_adjoint_batch(const kf_inputs_t *in, kf_adjoint_outputs_t *out, const
                          const kf_geometry_t *geo, const kf_field_t *field,
                          int32_t compute_gradient, void *workspace, size_t workspace_bytes,
                          void *stream) {
+  HostRange range("kf_adjoint_batch");
   int32_t rc = checkCommon(in, cfg, geo, field);
   if (rc) return rc;
   if (!out || !out->chi2 || !out->status)

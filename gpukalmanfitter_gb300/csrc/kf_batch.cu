@@ -193,6 +193,7 @@ namespace {
 int32_t enqueueBatched(const Params &P, const Variant *v, char *base, const BatchLayout &L,
                        cudaStream_t s) {
   if (P.n == 0) return KF_SUCCESS;
+  HostRange range("work-queue sort + persistent fit");
   cudaError_t e = cudaMemsetAsync(base + L.counter, 0, sizeof(int32_t), s);
   if (e != cudaSuccess) return cudaFail(e, "batched queue reset");
   const int32_t rc = sortQueue(P, reinterpret_cast<int32_t *>(base + L.hist),
@@ -299,6 +300,7 @@ int32_t kf_batch_plan_create(kf_batch_plan_t **plan, const kf_inputs_t *in, kf_o
 }
 
 int32_t kf_batch_plan_launch(kf_batch_plan_t *plan, void *stream) {
+  HostRange range("kf_batch_plan_launch");
   if (!plan || !plan->exec) return fail(KF_ERR_INVALID_ARGUMENT, "null plan%s");
   cudaError_t e = cudaGraphLaunch(plan->exec, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cudaFail(e, "graph launch");
@@ -316,6 +318,7 @@ int32_t kf_autotune(const kf_inputs_t *in, kf_outputs_t *out, const kf_config_t 
                     const kf_geometry_t *geo, const kf_field_t *field, void *workspace,
                     size_t workspace_bytes, void *stream, kf_config_t *tuned, double *best_ms) {
   if (!in || !cfg || !tuned) return fail(KF_ERR_INVALID_ARGUMENT, "null argument%s");
+  HostRange range("kf_autotune");
   // The first tracks (same stride) as the sample: at least several waves of
   // the resident grid, so that the queue's tail does not decide the timing.
   kf_inputs_t sample = *in;

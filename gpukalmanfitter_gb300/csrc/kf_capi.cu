@@ -202,6 +202,7 @@ size_t kf_workspace_size(const kf_config_t *cfg, int64_t n_tracks, int32_t n_sur
 int32_t kf_fit_batch(const kf_inputs_t *in, kf_outputs_t *out, const kf_config_t *cfg,
                      const kf_geometry_t *geo, const kf_field_t *field, void *workspace,
                      size_t workspace_bytes, void *stream) {
+  HostRange range("kf_fit_batch");
   int32_t rc = checkCommon(in, cfg, geo, field);
   if (rc) return rc;
   if (!out || !out->params || !out->cov || !out->chi2 || !out->status || !out->n_meas)
@@ -295,6 +296,7 @@ int32_t hostChunk(const kf_inputs_t *hin, kf_outputs_t *hout, const kf_config_t 
   auto chk = [&](cudaError_t x) {
     if (e == cudaSuccess) e = x;
   };
+  nvtxRangePushA("host-to-device copies");
   chk(copyRows(d + L.meas, cn, hin->meas + c0, hs, 8, cn, (size_t)S * 5, cudaMemcpyHostToDevice, s));
   if (hin->hit_mask)
     chk(cudaMemcpyAsync(d + L.mask, hin->hit_mask + c0, cn * 8, cudaMemcpyHostToDevice, s));
@@ -303,6 +305,7 @@ int32_t hostChunk(const kf_inputs_t *hin, kf_outputs_t *hout, const kf_config_t 
   chk(copyRows(d + L.start, cn, hin->start_params + c0, hs, 8, cn, 6, cudaMemcpyHostToDevice, s));
   chk(copyRows(d + L.scov, cn, hin->start_cov + c0, hs, 8, cn, 21, cudaMemcpyHostToDevice, s));
   chk(copyRows(d + L.perigee, cn, hin->perigee + c0, hs, 8, cn, 3, cudaMemcpyHostToDevice, s));
+  nvtxRangePop();
   if (e != cudaSuccess) return cudaFail(e, "host-to-device copy");
   kf_inputs_t din = *hin;
   din.n_tracks = cn;
@@ -327,6 +330,7 @@ int32_t hostChunk(const kf_inputs_t *hin, kf_outputs_t *hout, const kf_config_t 
                          ? kf_fit_batch_sorted(&din, &dout, cfg, geo, field, d + L.ws, wsb, s)
                          : kf_fit_batch(&din, &dout, cfg, geo, field, d + L.ws, wsb, s);
   if (rc) return rc;
+  HostRange copiesOut("device-to-host copies");
   const size_t os = hs; // host outputs share the input stride
   chk(copyRows(hout->params + c0, os, dout.params, cn, 8, cn, 6, cudaMemcpyDeviceToHost, s));
   chk(copyRows(hout->cov + c0, os, dout.cov, cn, 8, cn, 21, cudaMemcpyDeviceToHost, s));
@@ -368,6 +372,7 @@ size_t kf_host_staging_size(const kf_config_t *cfg, int64_t n_tracks, int32_t n_
 int32_t kf_fit_batch_host(const kf_inputs_t *hin, kf_outputs_t *hout, const kf_config_t *cfg,
                           const kf_geometry_t *geo, const kf_field_t *field, void *dev,
                           size_t bytes, void *stream) {
+  HostRange range("kf_fit_batch_host");
   int32_t rc = checkCommon(hin, cfg, geo, field);
   if (rc) return rc;
   if (!hout || !hout->params || !hout->cov || !hout->chi2 || !hout->status || !hout->n_meas)

@@ -2,10 +2,22 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include "kf_device.cuh"
 
 namespace kfh {
+
+// A named range on a profiler's host timeline around one phase of a call
+// (NVTX, header-only; without an attached tool a push or pop is a no-op
+// check).  The reference marks its fit the same way (PUSH_RANGE / POP_RANGE,
+// Utilities/Profiling.hpp:4-36, around Fitter/KalmanFitter.hpp:728-758).
+struct HostRange {
+  explicit HostRange(const char *name) { nvtxRangePushA(name); }
+  ~HostRange() { nvtxRangePop(); }
+  HostRange(const HostRange &) = delete;
+  HostRange &operator=(const HostRange &) = delete;
+};
 
 char *errorBuffer(); // thread-local text behind kf_last_error_string()
 int32_t fail(int32_t code, const char *fmt, const char *detail = "");

@@ -39,18 +39,47 @@ def balanced_ranges(keys: np.ndarray, world: int, chunk: int = CHUNK) -> list[np
 
 
 def subset(tel, idx: np.ndarray):
-    """A Telescope holding only the tracks idx (host arrays, same geometry)."""
+    """A Telescope holding only the tracks idx, in that order (same geometry
+    and field).  Host arrays stay numpy; the torch tensors of a telescope
+    simulated on the GPU are gathered on their device."""
     import copy
     t = copy.copy(tel)
     t.n = int(len(idx))
-    t.meas = np.ascontiguousarray(tel.meas[:, :, idx])
-    t.hit_mask = np.ascontiguousarray(tel.hit_mask[idx])
-    t.n_planes = np.ascontiguousarray(tel.n_planes[idx])
-    t.start = np.ascontiguousarray(tel.start[:, idx])
-    t.start_cov = np.ascontiguousarray(tel.start_cov[:, idx])
-    t.perigee = np.ascontiguousarray(tel.perigee[:, idx])
-    t.truth = np.ascontiguousarray(tel.truth[:, idx])
+    on_device = hasattr(tel.meas, "index_select")
+    if on_device:
+        import torch
+        di = torch.as_tensor(np.asarray(idx, dtype=np.int64), device=tel.meas.device)
+        take = lambda a: a.index_select(a.dim() - 1, di).contiguous()
+    else:
+        take = lambda a: np.ascontiguousarray(a[..., idx])
+    for k in ("meas", "hit_mask", "n_planes", "start", "start_cov", "perigee", "truth"):
+        setattr(t, k, take(getattr(tel, k)))
     return t
+
+
+def rank_tracks(tel, rank: int, world: int, chunk: int = CHUNK) -> np.ndarray:
+    """Track indices of `rank` in a batch split over `world` ranks by work
+    key (balanced_ranges); the keys come from the telescope's lengths and
+    start q/p, wherever its arrays live."""
+    lengths, qop = tel.n_planes, tel.start[4]
+    if hasattr(qop, "cpu"):
+        lengths, qop = lengths.cpu().numpy(), qop.cpu().numpy()
+    keys = work_keys(np.asarray(lengths), np.asarray(qop), tel.n_surfaces)
+    return balanced_ranges(keys, world, chunk)[rank]
+
+
+def place_tracks(parts, n: int) -> dict:
+    """Per-track results of several shards, [(track indices, {name: array
+    with the track axis last}), ...], put back into one batch of n tracks in
+    track order."""
+    out = {}
+    for ridx, res in parts:
+        for k, v in res.items():
+            v = np.asarray(v)
+            if k not in out:
+                out[k] = np.zeros(v.shape[:-1] + (n,), dtype=v.dtype)
+            out[k][..., np.asarray(ridx)] = v
+    return out
 
 
 def gather_tracks(local: dict, idx: np.ndarray, n: int, group=None) -> dict:
@@ -61,13 +90,7 @@ def gather_tracks(local: dict, idx: np.ndarray, n: int, group=None) -> dict:
     parts = [None] * world
     dist.all_gather_object(parts, (np.asarray(idx), {k: np.asarray(v) for k, v in local.items()}),
                            group=group)
-    out = {}
-    for ridx, res in parts:
-        for k, v in res.items():
-            if k not in out:
-                out[k] = np.zeros(v.shape[:-1] + (n,), dtype=v.dtype)
-            out[k][..., ridx] = v
-    return out
+    return place_tracks(parts, n)
 
 
 def reduce_gradients(grads: dict, group=None) -> dict:

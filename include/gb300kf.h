@@ -287,9 +287,12 @@ int32_t kf_autotune(const kf_inputs_t *in, kf_outputs_t *out,
  * KF_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until the
  * process exits.  A batch needing more scratch than that (kf_workspace_size)
  * is rejected with KF_ERR_WORKSPACE_TOO_SMALL and a message from
- * kf_noalloc_last_error_string(); split it or use kf_fit_batch.
+ * kf_noalloc_last_error_string() (this thread's last call; empty after a
+ * success); split it or use kf_fit_batch.
  * The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * (cudaGetSymbolAddress), and so does the first call after that device's
+ * context was replaced (cudaDeviceReset); make such a call before any stream
+ * capture.
  * All calls share the one array: calls that overlap on the GPU (different
  * streams, or host threads without ordering) race on it.  Nothing is
  * allocated, and nothing needs clearing between calls. */

@@ -1367,6 +1367,32 @@ int32_t oracle_material_interaction(const double matRow[6], int32_t flags, const
   return 0;
 }
 
+// The reference's fit defaults: maxSteps 1000 and maxRungeKuttaStepTrials
+// 10000 (Propagator/Propagator.hpp:76,79), the stepper tolerance 1e-4 and no
+// step-size cut-off (:92,95), the muon mass it never overrides (:73), the
+// 0.01 mm overstep limit (Propagator/EigenStepper.hpp:370), the 1e-4 mm
+// on-surface tolerance (Utilities/Definitions.hpp:41), smoothing on
+// (Fitter/KalmanFitter.hpp:89), no outlier rejection (the void outlier
+// finder, Fitter/detail/VoidKalmanComponents.hpp:67-80) and the stale
+// jacToGlobal after an update (Propagator/EigenStepper.ipp:554-564).
+void oracle_config_default(kf_config_t *c) {
+  if (!c) return;
+  std::memset(c, 0, sizeof(*c));
+  c->precision = KF_PRECISION_FP64;
+  c->max_steps = 1000;
+  c->max_rk_trials = 10000;
+  c->smoothing = 1;
+  c->tolerance = 1e-4;
+  c->step_size_cutoff = 0.;
+  c->mass = 105.6583755e-3;
+  c->overstep_limit = 0.01;
+  c->on_surface_tol = 1e-4;
+  c->outlier_chi2_cut = 0.;
+  c->faithful_jacobian = 1;
+  c->kernel = KF_KERNEL_AUTO;
+  c->block_size = 0;
+}
+
 int32_t oracle_num_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

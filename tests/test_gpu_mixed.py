@@ -51,3 +51,37 @@ def test_mixed_holes_outliers(kf, orc):
     assert np.mean(g["n_meas"] == o["n_meas"]) >= 0.999
     ok, rel = _errors(g, o)
     assert np.all(np.median(rel, axis=1) <= 1e-6), np.median(rel, axis=1)
+
+
+NAMES = ["d0", "z0", "phi", "theta", "qop", "t"]
+
+
+def test_config3_1M_map30_accuracy(kf, orc):
+    """The precision workload at its full size: 1M tracks of 30 planes in the
+    101^3 FP32 field map, batched mixed-precision form against the FP64
+    oracle.  Prints, per fitted parameter, the median, p99, p99.9 and max of
+    |mixed - FP64| / max(|FP64|, sigma), chi2's relative error and the pull
+    widths of both forms."""
+    tel = kf.make_telescope(1_000_000, n_planes=30, x_first=50., x_step=50., field_map=True,
+                            seed=1234567893)
+    b = kf.DeviceBatch(tel, kf.default_config(overstep_limit=0.1, precision=1))
+    b.fit_sorted()
+    g = b.results()
+    del b
+    o = orc.fit(tel, kf.default_config(overstep_limit=0.1), threads=0, variant="precise")
+    assert np.mean(g["status"] == o["status"]) >= 0.9999
+    assert np.mean(g["n_steps"] == o["n_steps"]) >= 0.999
+    ok, rel = _errors(g, o)
+    stats = {nm: {"median": float(np.median(rel[k])), "p99": float(np.percentile(rel[k], 99)),
+                  "p99.9": float(np.percentile(rel[k], 99.9)), "max": float(rel[k].max())}
+             for k, nm in enumerate(NAMES)}
+    c2 = np.abs(g["chi2"][ok] - o["chi2"][ok]) / np.maximum(o["chi2"][ok], 1e-300)
+    wg, wo = _pull_widths(g, tel, ok), _pull_widths(o, tel, ok)
+    print("mixed vs FP64, 1M map30:", stats)
+    print("chi2 rel: median", np.median(c2), "p99", np.percentile(c2, 99), "max", c2.max())
+    print("pull widths mixed", wg, "fp64", wo)
+    med = np.array([stats[nm]["median"] for nm in NAMES])
+    p99 = np.array([stats[nm]["p99"] for nm in NAMES])
+    assert np.all(med <= 1e-6), stats
+    assert np.all(p99 <= 2e-5), stats
+    assert np.all(np.abs(wg / wo - 1) < 0.01), (wg, wo)

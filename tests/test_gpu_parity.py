@@ -123,21 +123,55 @@ def test_empty_batch(kf):
     b.fit()  # no launch, no error
 
 
-def test_full_size_properties(kf):
-    """1M tracks: every track fits, pulls have unit width, reruns are bitwise
-    identical."""
+def test_config1_1M_parity(kf, orc):
+    """The headline workload at its full size, 1M tracks: the plain form
+    (one thread per track) and the batched form (sorted queue, persistent
+    kernel) each against the precise oracle at 1e-9, with identical status,
+    measurement, RK step and trial counts on every track; then the
+    size-independent properties: every track fits, unit pull widths, chi2 per
+    degree of freedom 1, and reruns bitwise identical."""
     import torch
     tel = kf.make_telescope(1_000_000, seed=2024)
     cfg = kf.default_config(overstep_limit=0.1)
     b = kf.DeviceBatch(tel, cfg)
     b.fit()
-    r1 = b.results()
+    plain = b.results()
+    b.fit_sorted()
+    batched = b.results()
+    o = orc.fit(tel, cfg, threads=0, variant="precise")
+    rep_plain = _compare(plain, o)
+    rep_batched = _compare(batched, o)
+    print("1M plain:", rep_plain, "1M batched:", rep_batched)
     b.fit()
     torch.cuda.synchronize()
-    r2 = b.results()
+    again = b.results()
     for k in ("params", "cov", "chi2", "status", "n_steps"):
-        assert np.array_equal(r1[k], r2[k])
-    assert np.all(r1["status"] == 0)
-    pulls = (r1["params"] - tel.truth) / np.sqrt(r1["cov"][DIAG])
+        assert np.array_equal(plain[k], again[k])
+    assert np.all(plain["status"] == 0)
+    pulls = (plain["params"] - tel.truth) / np.sqrt(plain["cov"][DIAG])
     assert np.all(np.abs(pulls[:5].std(axis=1) - 1) < 0.02)
-    assert abs(r1["chi2"].mean() / 20 - 1) < 0.01
+    assert abs(plain["chi2"].mean() / 20 - 1) < 0.01
+
+
+def test_config2_4M_batched_parity(kf, orc):
+    """The batching workload at its full size: 4M tracks of 30 planes with
+    uneven lengths U{5..30}, 10 % holes and 2 % outliers, fitted in one
+    batched launch (sorted queue, persistent kernel); every fourth track
+    (1M tracks) against the precise oracle at 1e-9 with identical control
+    flow, and the whole batch for its properties."""
+    from gpukalmanfitter_gb300 import shard
+    tel = kf.make_telescope(4_000_000, n_planes=30, x_first=50., x_step=50., min_len=5,
+                            max_len=30, hit_prob=0.9, outlier_prob=0.02, seed=1234567892)
+    cfg = kf.default_config(overstep_limit=0.1, outlier_chi2_cut=25.0)
+    b = kf.DeviceBatch(tel, cfg)
+    b.fit_sorted()
+    g = b.results()
+    del b
+    idx = np.arange(0, tel.n, 4)
+    o = orc.fit(shard.subset(tel, idx), cfg, threads=0, variant="precise")
+    rep = _compare({k: v[..., idx] for k, v in g.items()}, o)
+    print("4M batched, 1M checked:", rep)
+    ok = g["status"] == 0
+    assert ok.mean() > 0.999
+    hits = np.array([bin(int(m)).count("1") for m in tel.hit_mask[:20000]])
+    assert np.mean(g["n_meas"][:20000][ok[:20000]] == hits[ok[:20000]]) == 1.0

@@ -199,3 +199,19 @@ def test_reference_smoother_fp64_scatter(kf, orc):
     rep = parity_report(d, p, 1e-9)
     assert rep["params"] <= 1.0 and rep["chi2"] <= 1.0
     assert 1.0 < rep["cov"] < 100.0, rep
+
+
+def test_oracle_library_carries_the_same_defaults_and_generator(kf, orc):
+    """The reference arm of the benchmark builds its inputs and its fit
+    configuration from the oracle library alone; both must equal the product
+    library's, byte for byte."""
+    assert bytes(orc.default_config()) == bytes(kf.default_config())
+    assert bytes(orc.default_config(overstep_limit=0.1)) == bytes(kf.default_config(overstep_limit=0.1))
+    for kw in ({}, dict(n_planes=30, x_first=50., x_step=50., min_len=5, max_len=30, hit_prob=0.9,
+                        outlier_prob=0.02), dict(material=0.5),
+               dict(n_planes=20, x_first=50., x_step=50., mis_shift=0.1, mis_rot=1e-3)):
+        a = kf.make_telescope(1500, seed=12, **kw)
+        b = kf.make_telescope(1500, seed=12, lib=orc.load(), **kw)
+        for k in ("meas", "hit_mask", "n_planes", "start", "start_cov", "perigee", "truth",
+                  "center", "rotation", "truth_center", "truth_rotation"):
+            assert np.array_equal(getattr(a, k), getattr(b, k)), (kw, k)

@@ -65,3 +65,10 @@ def test_noalloc_rejects_batches_beyond_its_scratch(kf):
     assert rc == -2
     msg = lib.kf_noalloc_last_error_string().decode()
     assert "scratch" in msg and str(64 << 20) in msg
+    # a successful call after the refusal leaves no stale message behind
+    rc = lib.kf_fit_batch_noalloc(C.byref(b.ins), C.byref(b.outs), C.byref(cfg), C.byref(b.geo),
+                                  C.byref(b.field), None)
+    assert rc == 0
+    import torch
+    torch.cuda.synchronize()
+    assert lib.kf_noalloc_last_error_string().decode() == ""
