@@ -29,9 +29,9 @@ SYNTH_DEPS = [SYNTH_SRC, HERE.parent / "gpukalmanfitter_gb300" / "csrc" / "kf_sy
               HERE.parent / "gpukalmanfitter_gb300" / "csrc" / "kf_material.h",
               HERE.parent / "include" / "gb300kf_synth.h"]
 LIB = HERE / "_build" / "libkforacle.so"
-# Same source with the smoother evaluated in extended precision (long double):
-# the comparison point for the GPU (see the note on the smoother in
-# kf_oracle.cpp).
+# Same source with the smoother evaluated in double-double arithmetic (about
+# 106 bits, the same on every host): the comparison point for the GPU (see
+# the note on the smoother in kf_oracle.cpp).
 LIB_PRECISE = HERE / "_build" / "libkforacle_precise.so"
 HEADER = HERE.parent / "include" / "gb300kf.h"
 
@@ -56,9 +56,10 @@ def _compile(target: Path, flags: list[str], force: bool) -> Path:
 
 def build(force: bool = False, variant: str = "default") -> Path:
     """Compile the oracle.  ``variant="precise"`` evaluates the smoother in
-    long double; the default build is FP64 throughout (the CPU baseline)."""
+    double-double arithmetic; the default build is FP64 throughout (the CPU
+    baseline)."""
     if variant == "precise":
-        return _compile(LIB_PRECISE, ["-ffp-contract=off", "-DKFO_SMOOTHER_REAL=long double"], force)
+        return _compile(LIB_PRECISE, ["-ffp-contract=off", "-DKFO_SMOOTHER_DD"], force)
     return _compile(LIB, ["-ffp-contract=off"], force)
 
 

@@ -834,16 +834,93 @@ static bool hasNaN(const Mat<6, 6> &m) {
 // ---------------------------------------------------------------------------
 // Smoother arithmetic type.  The default build evaluates the reference
 // smoother in FP64, as the reference's double build does.  The "precise"
-// build (-DKFO_SMOOTHER_REAL="long double") evaluates the same formulas in
-// extended precision: the update C_s = C_f - G (C_p' - C_s') G^T cancels
-// heavily for the q/p variance, so FP64 evaluations of it scatter by 1e-9 to
-// 5e-8 relative; the extended evaluation is close to the formula's exact
-// value and is the comparison point for the GPU.
+// build (-DKFO_SMOOTHER_DD) evaluates the same formulas in double-double
+// arithmetic (about 106 significant bits): the update
+// C_s = C_f - G (C_p' - C_s') G^T cancels heavily for the q/p variance, so
+// FP64 evaluations of it scatter by 1e-9 to 5e-8 relative; the double-double
+// evaluation is close to the formula's exact value and is the comparison
+// point for the GPU.  It is built from IEEE double operations alone
+// (error-free sums, Dekker's split product; the oracle is compiled without
+// FMA contraction), so it gives the same bits on every host, and it runs at
+// a few times the FP64 cost where a software quad would cost ten times more.
 // ---------------------------------------------------------------------------
+#if defined(KFO_SMOOTHER_DD)
+struct DD {
+  double hi = 0., lo = 0.;
+  DD() = default;
+  DD(double x) : hi(x), lo(0.) {}
+  DD(int x) : hi((double)x), lo(0.) {}
+  static DD norm(double s, double e) { // |e| <= ulp(s) / 2 afterwards
+    const double h = s + e;
+    DD r;
+    r.hi = h;
+    r.lo = e - (h - s);
+    return r;
+  }
+  static void twoSum(double a, double b, double &s, double &e) {
+    s = a + b;
+    const double bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+  }
+  static void split(double a, double &h, double &l) {
+    const double t = 134217729.0 * a; // 2^27 + 1
+    h = t - (t - a);
+    l = a - h;
+  }
+  static void twoProd(double a, double b, double &p, double &e) {
+    p = a * b;
+    double ah, al, bh, bl;
+    split(a, ah, al);
+    split(b, bh, bl);
+    e = ((ah * bh - p) + ah * bl + al * bh) + al * bl;
+  }
+  explicit operator double() const { return hi; }
+  friend DD operator+(const DD &a, const DD &b) {
+    double s, e, t, f;
+    twoSum(a.hi, b.hi, s, e);
+    twoSum(a.lo, b.lo, t, f);
+    e += t;
+    DD r = norm(s, e);
+    return norm(r.hi, r.lo + f);
+  }
+  friend DD operator-(const DD &a) {
+    DD r;
+    r.hi = -a.hi;
+    r.lo = -a.lo;
+    return r;
+  }
+  friend DD operator-(const DD &a, const DD &b) { return a + (-b); }
+  friend DD operator*(const DD &a, const DD &b) {
+    double p, e;
+    twoProd(a.hi, b.hi, p, e);
+    e += a.hi * b.lo + a.lo * b.hi;
+    return norm(p, e);
+  }
+  friend DD operator/(const DD &a, const DD &b) {
+    const double q1 = a.hi / b.hi;
+    DD r = a - b * DD(q1);
+    const double q2 = r.hi / b.hi;
+    r = r - b * DD(q2);
+    const double q3 = r.hi / b.hi;
+    const DD q = norm(q1, q2);
+    return q + DD(q3);
+  }
+  DD &operator+=(const DD &b) { return *this = *this + b; }
+  DD &operator-=(const DD &b) { return *this = *this - b; }
+  DD &operator*=(const DD &b) { return *this = *this * b; }
+  DD &operator/=(const DD &b) { return *this = *this / b; }
+  friend bool operator<(const DD &a, const DD &b) {
+    return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo);
+  }
+  friend bool operator>(const DD &a, const DD &b) { return b < a; }
+};
+typedef DD SReal;
+#else
 #ifndef KFO_SMOOTHER_REAL
 #define KFO_SMOOTHER_REAL double
 #endif
 typedef KFO_SMOOTHER_REAL SReal;
+#endif
 struct M6 {
   SReal a[6][6];
 };
