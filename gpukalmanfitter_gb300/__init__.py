@@ -149,6 +149,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.kf_synth_field_map.argtypes = [C.c_double, C.c_int32, C.c_double, C.c_void_p]
     lib.kf_synth_tracks.restype = C.c_int32
     lib.kf_simulate_tracks.restype = C.c_int32
+    lib.kf_field_map_read_rz_native.restype = C.c_int32
     _LIB = lib
     return lib
 
@@ -200,6 +201,7 @@ class Telescope:
     field_dims: tuple | None = None
     field_min: tuple | None = None
     field_max: tuple | None = None
+    field_kind: int = 1                     # kf_field_kind of a grid field
     synth_cfg: object = None                # SynthConfig of a GPU-simulated telescope
 
     def geometry(self) -> tuple[KfGeometry, tuple]:
@@ -216,7 +218,7 @@ class Telescope:
             f.kind = 0
             f.value[0], f.value[1], f.value[2] = 0.0, 0.0, self.bz_tesla * TESLA
         else:
-            f.kind = 1
+            f.kind = self.field_kind
             if self.field_dims is not None:
                 f.nx, f.ny, f.nz = self.field_dims
                 for a in range(3):
@@ -339,6 +341,7 @@ def make_telescope(n: int, *, seed: int = 1234567890, n_planes: int = 10,
         tel.field_dims = tuple(field_map.dims)
         tel.field_min = tuple(field_map.min)
         tel.field_max = tuple(field_map.max)
+        tel.field_kind = int(getattr(field_map, "kind", 1))
     if field_map is not None and field_map is not False:
         field = tel.field(grid.data_ptr() if device is not None else None)
     if device is not None:

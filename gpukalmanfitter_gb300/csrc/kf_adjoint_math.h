@@ -940,12 +940,12 @@ KF_HD void boundFwd(const BoundIn &in, const Frame &f, BoundOut &o, BoundTmp &w,
   for (int i = 0; i < 3; ++i) dd[i] = in.pos[i] - f.c[i];
   o.pred[0] = dot(f.U, dd);
   o.pred[1] = dot(f.V, dd);
-  const double pabs = fabs(1. / (in.q / in.p));
-  double mom[3] = {pabs * in.dir[0], pabs * in.dir[1], pabs * in.dir[2]};
-  const double pt = sqrt(mom[0] * mom[0] + mom[1] * mom[1]);
-  o.pred[2] = atan2(mom[1], mom[0]);
-  o.pred[3] = atan2(pt, mom[2]);
-  o.pred[4] = (in.q > 0. ? 1. : -1.) / sqrt(dot(mom, mom));
+  // angles from the direction, q/p as the stepper holds it (the fit's
+  // boundAngles)
+  const double pt = sqrt(in.dir[0] * in.dir[0] + in.dir[1] * in.dir[1]);
+  o.pred[2] = atan2(in.dir[1], in.dir[0]);
+  o.pred[3] = atan2(pt, in.dir[2]);
+  o.pred[4] = in.q / in.p;
   o.pred[5] = in.t;
 }
 
@@ -994,9 +994,8 @@ KF_HD void boundVjp(const BoundIn &in, const Frame &f, const BoundOut &o, const 
     ib.dir[2] += ob.pred[3] * (-s * irho2);
     ib.dir[0] += sb * x * is;
     ib.dir[1] += sb * y * is;
-    // q/p = charge / (p |d|), |d|^2 = rho2
+    // q/p = q / p
     ib.p += ob.pred[4] * (-o.pred[4] / in.p);
-    for (int i = 0; i < 3; ++i) ib.dir[i] += ob.pred[4] * (-o.pred[4] * in.dir[i] * irho2);
   }
   ib.t += ob.pred[5];
   // ---- new jacToGlobal
@@ -1206,7 +1205,7 @@ KF_HD void filterVjp(const double C[21], const FilterTmp &w, const double filtb[
 // Stepper update from filtered plane parameters (EigenStepper.ipp:554-564,
 // coordinate_transformations.hpp:145-158) and the per-leg constants
 //   pos = c + U x0 + V x1, d = unit(cos x2 sin x3, sin x2 sin x3, cos x3),
-//   p = |1/x4|, t = x5;  qop = q/p, dtds = hypot(1, m/p), d37 = m^2 q/(p dtds)
+//   p = |1/x4|, t = x5;  qop = q/p, dtds = sqrt(1 + (m/p)^2), d37 = m^2 q/(p dtds)
 // ---------------------------------------------------------------------------
 KF_HD void updateFwd(const Frame &f, const double x[6], double pos[3], double d[3], double *p,
                      double *t, double trig[4] = nullptr) {
@@ -1252,10 +1251,17 @@ struct Leg {
   double qop, dtds, d37;
 };
 KF_HD void legFwd(double p, double q, double mass, Leg &g) {
+  // the fit's legConstantsIp: one 1/sqrt(1 + (m/p)^2)
   const double ip = 1. / p;
   g.qop = q * ip;
-  g.dtds = hypot(1., mass * ip);
-  g.d37 = mass * mass * q * ip / g.dtds;
+  const double x = mass * ip, a = 1. + x * x;
+#ifdef __CUDA_ARCH__
+  const double y = rsqrt(a);
+#else
+  const double y = 1. / sqrt(a);
+#endif
+  g.dtds = a * y;
+  g.d37 = mass * mass * q * ip * y;
 }
 KF_HD void legVjp(double p, double q, double mass, const Leg &g, double qopb, double dtdsb,
                   double d37b, double &pb) {

@@ -56,11 +56,16 @@ int32_t checkCommon(const kf_inputs_t *in, const kf_config_t *cfg, const kf_geom
   if (in->n_surfaces <= 0 || in->n_surfaces > KF_MAX_PLANES || geo->n_planes < in->n_surfaces)
     return fail(KF_ERR_INVALID_ARGUMENT, "bad n_surfaces (1..64, <= geometry planes)%s");
   if (!geo->center || !geo->rotation) return fail(KF_ERR_INVALID_ARGUMENT, "null geometry%s");
-  if (field->kind != KF_FIELD_CONSTANT && field->kind != KF_FIELD_GRID3D)
+  if (field->kind != KF_FIELD_CONSTANT && field->kind != KF_FIELD_GRID3D &&
+      field->kind != KF_FIELD_GRID_RZ)
     return fail(KF_ERR_INVALID_ARGUMENT, "unknown field kind%s");
   if (field->kind == KF_FIELD_GRID3D &&
       (!field->grid || field->nx < 2 || field->ny < 2 || field->nz < 2))
     return fail(KF_ERR_INVALID_ARGUMENT, "bad field grid%s");
+  if (field->kind == KF_FIELD_GRID_RZ &&
+      (!field->grid || field->nx < 2 || field->nz < 2 || !(field->max[0] > field->min[0]) ||
+       !(field->max[2] > field->min[2])))
+    return fail(KF_ERR_INVALID_ARGUMENT, "bad (r, z) field grid%s");
   if (cfg->precision != KF_PRECISION_FP64 && cfg->precision != KF_PRECISION_MIXED)
     return fail(KF_ERR_UNSUPPORTED, "unknown precision mode%s");
   if (cfg->max_steps < 0 || cfg->max_rk_trials < 0)
@@ -110,10 +115,13 @@ void fillParams(Params &P, const kf_inputs_t *in, const kf_outputs_t *out, const
   F.n[0] = field->nx;
   F.n[1] = field->ny;
   F.n[2] = field->nz;
-  if (field->kind == KF_FIELD_GRID3D) {
+  if (field->kind == KF_FIELD_GRID3D || field->kind == KF_FIELD_GRID_RZ) {
     for (int a = 0; a < 3; ++a) {
       const int na = (a == 0) ? field->nx : (a == 1) ? field->ny : field->nz;
-      F.invw[a] = (na - 1) / (field->max[a] - field->min[a]);
+      // the (r, z) grid has no y axis
+      F.invw[a] = (field->kind == KF_FIELD_GRID_RZ && a == 1)
+                      ? 0.
+                      : (na - 1) / (field->max[a] - field->min[a]);
     }
   }
   F.grid = reinterpret_cast<const float4 *>(field->grid);
@@ -122,7 +130,7 @@ void fillParams(Params &P, const kf_inputs_t *in, const kf_outputs_t *out, const
     F.Blo[a] = (float)(F.B[a] - (double)F.Bf[a]);
     F.mnf[a] = (float)F.mn[a];
     F.invwf[a] = (float)F.invw[a];
-    F.wf[a] = field->kind == KF_FIELD_GRID3D ? (float)(1. / F.invw[a]) : 0.f;
+    F.wf[a] = (field->kind != KF_FIELD_CONSTANT && F.invw[a] != 0.) ? (float)(1. / F.invw[a]) : 0.f;
   }
   F.scalef = (float)F.scale;
   F.scalelo = (float)(F.scale - (double)F.scalef);

@@ -116,11 +116,43 @@ enum { PC_PRE = 0, PC_LOOP = 1, PC_ACT = 2, PC_POST = 3, PC_DONE = 4 };
 // trilinear map (MagneticField/InterpolatedBFieldMap.hpp:178-181), in FP64
 // (plain form) or FP32 pairs (mixed form, getFieldFF).
 // ---------------------------------------------------------------------------
+// (r, z) map (fieldMapperRZ, MagneticField/BFieldMapUtils.cpp:17-136): the
+// (br, bz) grid interpolated bilinearly at r = |(x, y)| (in r, then in z), and
+// br turned by the position's azimuth (cos phi = x / r, sin phi = y / r; phi =
+// 0 on the axis, the reference's transformBField)
+static __device__ __noinline__ void getFieldRZ(const FieldD &F, const double p[3], double B[3]) {
+  const double r2 = p[0] * p[0] + p[1] * p[1];
+  const double r = sqrt(r2);
+  const double gr = (r - F.mn[0]) * F.invw[0], gz = (p[2] - F.mn[2]) * F.invw[2];
+  const int ir = min(max((int)floor(gr), 0), F.n[0] - 2);
+  const int iz = min(max((int)floor(gz), 0), F.n[2] - 2);
+  const double fr = gr - ir, fz = gz - iz;
+  const size_t nr = F.n[0], base = (size_t)iz * nr + ir;
+  const float4 v00 = __ldg(F.grid + base), v10 = __ldg(F.grid + base + 1);
+  const float4 v01 = __ldg(F.grid + base + nr), v11 = __ldg(F.grid + base + nr + 1);
+  const double hr = 1 - fr, hz = 1 - fz;
+  const double br = ((v00.x * hr + v10.x * fr) * hz + (v01.x * hr + v11.x * fr) * fz) * F.scale;
+  const double bz = ((v00.y * hr + v10.y * fr) * hz + (v01.y * hr + v11.y * fr) * fz) * F.scale;
+  double cphi = 1., sphi = 0.;
+  if (r2 > DBL_MIN) {
+    const double inv = 1. / r;
+    cphi = p[0] * inv;
+    sphi = p[1] * inv;
+  }
+  B[0] = br * cphi;
+  B[1] = br * sphi;
+  B[2] = bz;
+}
+
 __device__ __forceinline__ void getField(const FieldD &F, const double p[3], double B[3]) {
   if (F.kind == KF_FIELD_CONSTANT) {
     B[0] = F.B[0];
     B[1] = F.B[1];
     B[2] = F.B[2];
+    return;
+  }
+  if (F.kind == KF_FIELD_GRID_RZ) {
+    getFieldRZ(F, p, B);
     return;
   }
   int idx[3];
@@ -162,21 +194,71 @@ __device__ __forceinline__ void getField(const FieldD &F, const double p[3], dou
 // interpolation runs in FP32 on the corner values' differences from the
 // lower corner, v - v000, and adds v000 back as a pair: its rounding errors
 // scale with the field's variation across the cell, not with the field.
-__device__ __forceinline__ void getFieldFF(const FieldD &F, const float p[3], kff::ff B[3]) {
+// Mixed form of the (r, z) lookup: weights from the offsets to the cell's
+// lower corner, the interpolation on the corner values' differences from the
+// lower corner with the corner added back as a pair (as getFieldFF), and the
+// azimuth's cosine and sine in FP32
+static __device__ __noinline__ void getFieldFFRZ(const FieldD &F, const float p[3], kff::ff B[3]) {
+  const float r2 = p[0] * p[0] + p[1] * p[1];
+  const float r = sqrtf(r2);
+  const float gr = (r - F.mnf[0]) * F.invwf[0], gz = (p[2] - F.mnf[2]) * F.invwf[2];
+  const int ir = min(max((int)floorf(gr), 0), F.n[0] - 2);
+  const int iz = min(max((int)floorf(gz), 0), F.n[2] - 2);
+  const float fr = __fmul_rn(__fsub_rn(r, __fmaf_rn((float)ir, F.wf[0], F.mnf[0])), F.invwf[0]);
+  const float fz = __fmul_rn(__fsub_rn(p[2], __fmaf_rn((float)iz, F.wf[2], F.mnf[2])), F.invwf[2]);
+  const size_t nr = F.n[0], base = (size_t)iz * nr + ir;
+  const float4 v00 = __ldg(F.grid + base), v10 = __ldg(F.grid + base + 1);
+  const float4 v01 = __ldg(F.grid + base + nr), v11 = __ldg(F.grid + base + nr + 1);
+  const kff::ff sc = {F.scalef, F.scalelo};
+  auto bil = [&](float a00, float a10, float a01, float a11) {
+    const float d01 = a01 - a00;
+    const float c0 = fr * (a10 - a00);
+    const float c1 = d01 + fr * ((a11 - a00) - d01);
+    return kff::mul(kff::twoSum(a00, c0 + fz * (c1 - c0)), sc);
+  };
+  const kff::ff br = bil(v00.x, v10.x, v01.x, v11.x);
+  B[2] = bil(v00.y, v10.y, v01.y, v11.y);
+  float cphi = 1.f, sphi = 0.f;
+  if (r2 > FLT_MIN) {
+    const float inv = 1.f / r;
+    cphi = p[0] * inv;
+    sphi = p[1] * inv;
+  }
+  B[0] = kff::mul(br, {cphi, 0.f});
+  B[1] = kff::mul(br, {sphi, 0.f});
+}
+
+//
+// The position is given as at + inc: `at` an FP32 position (the step's
+// start rounded to FP32), inc a small FP32 offset from it (that rounding's
+// residual plus the trial increment).  The offset to the corner is formed as
+// (at - corner) + inc: at - corner is exact (two FP32 values a few cells
+// apart, the corner on the grid), so the weights carry only the rounding of a
+// cell-sized number instead of the position's (6e-5 mm at 1 m, which moves
+// the fitted d0 by up to 1e-5 of its resolution on the 30-plane map
+// telescope).
+__device__ __forceinline__ void getFieldFF(const FieldD &F, const float at[3],
+                                           const float inc[3], kff::ff B[3]) {
   if (F.kind == KF_FIELD_CONSTANT) {
 #pragma unroll
     for (int a = 0; a < 3; ++a) B[a] = {F.Bf[a], F.Blo[a]};
+    return;
+  }
+  if (F.kind == KF_FIELD_GRID_RZ) {
+    const float p[3] = {at[0] + inc[0], at[1] + inc[1], at[2] + inc[2]};
+    getFieldFFRZ(F, p, B);
     return;
   }
   int idx[3];
   float f[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    const float g = (p[a] - F.mnf[a]) * F.invwf[a];
+    const float g = ((at[a] + inc[a]) - F.mnf[a]) * F.invwf[a];
     int i = (int)floorf(g);
     i = min(max(i, 0), F.n[a] - 2);
     idx[a] = i;
-    f[a] = __fmul_rn(__fsub_rn(p[a], __fmaf_rn((float)i, F.wf[a], F.mnf[a])), F.invwf[a]);
+    const float d = __fsub_rn(at[a], __fmaf_rn((float)i, F.wf[a], F.mnf[a]));
+    f[a] = __fmul_rn(__fadd_rn(d, inc[a]), F.invwf[a]);
   }
   const size_t nx = F.n[0], nxy = (size_t)F.n[0] * F.n[1];
   const size_t base = (size_t)idx[2] * nxy + (size_t)idx[1] * nx + idx[0];
@@ -343,21 +425,19 @@ __device__ __forceinline__ double rsqrtNewton(double a) {
 }
 
 // per-leg constants from 1/p (ip): q/p, dt/ds = sqrt(1 + (m/p)^2) and the
-// transport matrix's time-q/p factor m^2 q / (p dt/ds).  The plain form
-// follows the reference's expressions; the mixed form spends no FP64
-// division on them.
+// transport matrix's time-q/p factor m^2 q / (p dt/ds), through one
+// 1/sqrt(1 + (m/p)^2) (the reference's hypot and division, EigenStepper.ipp:
+// 36-47, :110-112, to an ulp): an FP64 rsqrt in the plain form, an FP32
+// estimate refined in FP64 in the mixed form.
 template <typename R, typename H>
 __device__ __forceinline__ void legConstantsIp(Lane<R, H> &L, double mass, double ip) {
   L.qop = L.q * ip;
-  if constexpr (sizeof(R) == sizeof(float)) {
-    const double x = mass * ip, a = 1. + x * x;
-    const double y = rsqrtNewton(a);
-    L.dtds = a * y;
-    L.d37 = mass * mass * L.q * ip * y;
-  } else {
-    L.dtds = hypot(1., mass * ip);
-    L.d37 = mass * mass * L.q * ip / L.dtds;
-  }
+  const double x = mass * ip, a = 1. + x * x;
+  double y;
+  if constexpr (sizeof(R) == sizeof(float)) y = rsqrtNewton(a);
+  else y = rsqrt(a);
+  L.dtds = a * y;
+  L.d37 = mass * mass * L.q * ip * y;
 }
 template <typename R, typename H> __device__ __forceinline__ void legConstants(Lane<R, H> &L, double mass) {
   legConstantsIp(L, mass, 1. / L.p);
@@ -379,12 +459,28 @@ template <typename R, typename H> __device__ __forceinline__ void resetTransport
   L.stepped = false;
 }
 
-// PlaneSurface::initJacobianToGlobal (PlaneSurface.ipp:122-156)
-template <typename R, typename H> __device__ __forceinline__ void planeJacToGlobal(Lane<R, H> &L, const PlaneD &pl) {
+// cos and sin of the direction's phi and theta from its components
+// (cos theta = z, sin theta = |(x, y)|, cos phi = x / sin theta, ...), with
+// 1 / sin theta: shared by the bound Jacobian at a surface and the
+// re-initialised jacToGlobal there, which see the same direction
+template <typename R> struct DirTrig {
+  R cosT, sinT, invS, cosP, sinP;
+};
+template <typename R, typename H> __device__ __forceinline__ DirTrig<R> dirTrig(const Lane<R, H> &L) {
+  DirTrig<R> t;
   const R x = (R)L.dir[0], y = (R)L.dir[1], z = (R)L.dir[2];
-  const R cosT = z, sinT = sqrt(x * x + y * y);
-  const R inv = R(1) / sinT;
-  const R cosP = x * inv, sinP = y * inv;
+  t.cosT = z;
+  t.sinT = sqrt(x * x + y * y);
+  t.invS = R(1) / t.sinT;
+  t.cosP = x * t.invS;
+  t.sinP = y * t.invS;
+  return t;
+}
+
+// PlaneSurface::initJacobianToGlobal (PlaneSurface.ipp:122-156)
+template <typename R, typename H>
+__device__ __forceinline__ void planeJacToGlobal(Lane<R, H> &L, const PlaneD &pl, const DirTrig<R> &tr) {
+  const R cosT = tr.cosT, sinT = tr.sinT, cosP = tr.cosP, sinP = tr.sinP;
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
     L.g03(r, 0) = (R)pl.U[r];
@@ -398,6 +494,9 @@ template <typename R, typename H> __device__ __forceinline__ void planeJacToGlob
   L.g46(1, 1) = cosT * sinP;
   L.g46(2, 0) = R(0);
   L.g46(2, 1) = (-sinT);
+}
+template <typename R, typename H> __device__ __forceinline__ void planeJacToGlobal(Lane<R, H> &L, const PlaneD &pl) {
+  planeJacToGlobal(L, pl, dirTrig(L));
 }
 
 // LineSurface::referenceFrame (LineSurface.ipp:46-61), line axis z
@@ -484,9 +583,10 @@ struct StagesDelta {
   float dBm[3], d2[3], d3[3], d4[3];
 };
 
-__device__ __forceinline__ void rkFirstDelta(const FieldD &F, const float posf[3], const double dir[3],
-                                             double qop, StagesDelta &S) {
-  getFieldFF(F, posf, S.Bf);
+// posf: the step's start rounded to FP32, res: that rounding's residual
+__device__ __forceinline__ void rkFirstDelta(const FieldD &F, const float posf[3], const float res[3],
+                                             const double dir[3], double qop, StagesDelta &S) {
+  getFieldFF(F, posf, res, S.Bf);
   double B[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
@@ -503,15 +603,15 @@ __device__ __forceinline__ void rkFirstDelta(const FieldD &F, const float posf[3
 }
 
 // tryRungeKuttaStep (EigenStepper.ipp:243-269) as FP32 offsets from k1; the
-// trial positions only locate the field
-__device__ __forceinline__ float rkTrialDelta(const FieldD &F, const float pos[3], const float dir[3],
-                                              float q, float h, StagesDelta &S) {
+// trial positions (pos + res + increment) only locate the field
+__device__ __forceinline__ float rkTrialDelta(const FieldD &F, const float pos[3], const float res[3],
+                                              const float dir[3], float q, float h, StagesDelta &S) {
   const float h2 = h * h, half_h = h * 0.5f;
   float p1[3], dB[3], a[3], b[3];
   kff::ff B[3];
 #pragma unroll
-  for (int i = 0; i < 3; ++i) p1[i] = pos[i] + half_h * dir[i] + (h2 * 0.125f) * S.s.k1[i];
-  getFieldFF(F, p1, B);
+  for (int i = 0; i < 3; ++i) p1[i] = res[i] + half_h * dir[i] + (h2 * 0.125f) * S.s.k1[i];
+  getFieldFF(F, pos, p1, B);
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     S.s.Bm[i] = B[i].hi;
@@ -531,8 +631,8 @@ __device__ __forceinline__ float rkTrialDelta(const FieldD &F, const float pos[3
     S.s.k3[i] = S.s.k1[i] + S.d3[i];
   }
 #pragma unroll
-  for (int i = 0; i < 3; ++i) p1[i] = pos[i] + h * dir[i] + (h2 * 0.5f) * S.s.k3[i];
-  getFieldFF(F, p1, B);
+  for (int i = 0; i < 3; ++i) p1[i] = res[i] + h * dir[i] + (h2 * 0.5f) * S.s.k3[i];
+  getFieldFF(F, pos, p1, B);
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     S.s.Bl[i] = B[i].hi;
@@ -741,13 +841,15 @@ template <typename R, typename H> __device__ void rkStep(Lane<R, H> &L, const Pa
     // ---- mixed form: FP32 stage offsets from an FP64 k1, FP32 transport
     const float qopf = (float)L.qop;
     const float posf[3] = {(float)L.pos[0], (float)L.pos[1], (float)L.pos[2]};
+    const float res[3] = {(float)(L.pos[0] - (double)posf[0]), (float)(L.pos[1] - (double)posf[1]),
+                          (float)(L.pos[2] - (double)posf[2])};
     const float dirf[3] = {(float)L.dir[0], (float)L.dir[1], (float)L.dir[2]};
     const float tolLo = P.tolLoF, tolHi = P.tolHiF;
     StagesDelta S;
-    rkFirstDelta(P.field, posf, L.dir, L.qop, S);
+    rkFirstDelta(P.field, posf, res, L.dir, L.qop, S);
     for (;;) {
       L.rkTrials++;
-      const float errf = rkTrialDelta(P.field, posf, dirf, qopf, (float)h, S);
+      const float errf = rkTrialDelta(P.field, posf, res, dirf, qopf, (float)h, S);
       double err = errf;
       bool accept;
       if (errf <= tolLo) {
@@ -843,7 +945,8 @@ __device__ __forceinline__ void applyTransport(const Lane<R, H> &L, Transported<
 // PlaneSurface.ipp:158-189 / LineSurface.ipp:114-143.
 template <typename R, typename H>
 __device__ __forceinline__ void projectCov(Lane<R, H> &L, Transported<R> &X, const R sVec[5],
-                                           const R ax0[3], const R ax1[3], double Jst[25]) {
+                                           const R ax0[3], const R ax1[3], const DirTrig<R> &tr,
+                                           double Jst[25]) {
   // derivative (EigenStepper.ipp:320-325): direction, dt/ds and k4 of the
   // last step; zero right after a Jacobian reset
   R der[7];
@@ -862,10 +965,7 @@ __device__ __forceinline__ void projectCov(Lane<R, H> &L, Transported<R> &X, con
     }
     X.R3[c] -= der[3] * sVec[c];
   }
-  const R x = (R)L.dir[0], y = (R)L.dir[1], z = (R)L.dir[2];
-  const R cosT = z, sinT = sqrt(x * x + y * y);
-  const R invS = R(1) / sinT;
-  const R cosP = x * invS, sinP = y * invS;
+  const R cosT = tr.cosT, sinT = tr.sinT, invS = tr.invS, cosP = tr.cosP, sinP = tr.sinP;
   const R j24 = -sinP * invS, j25 = cosP * invS;
   const R j34 = cosP * cosT, j35 = sinP * cosT, j36 = -sinT;
   // the Jacobian's arithmetic type: FP32 in the mixed form (Jacobian
@@ -959,36 +1059,33 @@ __device__ __forceinline__ void projectCov(Lane<R, H> &L, Transported<R> &X, con
 }
 
 // BoundParameters from the free state (CovarianceEngine.hpp:363-370 and
-// coordinate_transformations.hpp:115-128): angles and q/p from the momentum.
+// coordinate_transformations.hpp:115-128): angles from the momentum
+// direction, |p| and q/p as the stepper holds them.  The reference forms q/p
+// as charge / |p d| with p = |1 / (q/p)|; with |d| = 1 that is the stepper's
+// q/p to an ulp, without the three divisions and the square root.
+//
+// With absAngles == false the angles are given as offsets from the
+// direction's own angles, i.e. 0 (see filterHit).
 template <typename R, typename H>
-__device__ __forceinline__ void boundAngles(const Lane<R, H> &L, double out[6], double mom[3]) {
-  if constexpr (sizeof(R) == sizeof(float)) {
-    // mixed form: |p| and q/p as the stepper holds them (no FP64 division)
+__device__ __forceinline__ void boundAngles(const Lane<R, H> &L, double out[6], double mom[3],
+                                            bool absAngles = true) {
 #pragma unroll
-    for (int i = 0; i < 3; ++i) mom[i] = L.p * L.dir[i];
+  for (int i = 0; i < 3; ++i) mom[i] = L.p * L.dir[i];
+  if (absAngles) {
     out[2] = atan2(L.dir[1], L.dir[0]);
     out[3] = atan2(sqrt(L.dir[0] * L.dir[0] + L.dir[1] * L.dir[1]), L.dir[2]);
-    out[4] = L.qop;
-    out[5] = L.t;
-    return;
+  } else {
+    out[2] = 0.;
+    out[3] = 0.;
   }
-  const double qopF = L.q / L.p;
-  const double pabs = fabs(1. / qopF);
-  mom[0] = pabs * L.dir[0];
-  mom[1] = pabs * L.dir[1];
-  mom[2] = pabs * L.dir[2];
-  const double charge = copysign(1., qopF);
-  const double pt = sqrt(mom[0] * mom[0] + mom[1] * mom[1]);
-  out[2] = atan2(mom[1], mom[0]);
-  out[3] = atan2(pt, mom[2]);
-  out[4] = ((fabs(charge) < 1e-4) ? 1. : charge) /
-           sqrt(mom[0] * mom[0] + mom[1] * mom[1] + mom[2] * mom[2]);
+  out[4] = L.qop;
   out[5] = L.t;
 }
 
 // boundState<PlaneSurface> (EigenStepper.ipp:516-540) incl. re-initialisation
 template <typename R, typename H>
-__device__ void boundStatePlane(Lane<R, H> &L, const PlaneD &pl, double out[6], double Jst[25]) {
+__device__ void boundStatePlane(Lane<R, H> &L, const PlaneD &pl, double out[6], double Jst[25],
+                                bool absAngles = true) {
   Transported<R> X;
   applyTransport(L, X);
   // PlaneSurface::derivativeFactors (PlaneSurface.ipp:191-204)
@@ -1001,15 +1098,16 @@ __device__ void boundStatePlane(Lane<R, H> &L, const PlaneD &pl, double out[6], 
   for (int c = 0; c < 5; ++c) sVec[c] = nv0 * X.Pt[0][c] + nv1 * X.Pt[1][c] + nv2 * X.Pt[2][c];
   const R U[3] = {(R)pl.U[0], (R)pl.U[1], (R)pl.U[2]};
   const R V[3] = {(R)pl.V[0], (R)pl.V[1], (R)pl.V[2]};
-  projectCov(L, X, sVec, U, V, Jst);
+  const DirTrig<R> tr = dirTrig(L);
+  projectCov(L, X, sVec, U, V, tr, Jst);
   // reinitializeJacobians (CovarianceEngine.hpp:169-201)
   resetTransport(L);
-  planeJacToGlobal(L, pl);
+  planeJacToGlobal(L, pl, tr);
   const double d0 = L.pos[0] - pl.c[0], d1 = L.pos[1] - pl.c[1], d2 = L.pos[2] - pl.c[2];
   out[0] = pl.U[0] * d0 + pl.U[1] * d1 + pl.U[2] * d2;
   out[1] = pl.V[0] * d0 + pl.V[1] * d1 + pl.V[2] * d2;
   double mom[3];
-  boundAngles(L, out, mom);
+  boundAngles(L, out, mom, absAngles);
 }
 
 // boundState<LineSurface> towards the perigee line (axis z through `c`)
@@ -1037,7 +1135,7 @@ __device__ void boundStateLine(Lane<R, H> &L, const double c[3], double out[6]) 
     sVec[k] = nrm * (s - row);
   }
   double Jst[25];
-  projectCov(L, X, sVec, rX, rY, Jst);
+  projectCov(L, X, sVec, rX, rY, dirTrig(L), Jst);
   double mom[3];
   boundAngles(L, out, mom);
   // LineSurface::globalToLocal (LineSurface.ipp:200-220)
@@ -1069,8 +1167,7 @@ __device__ __forceinline__ void stepperUpdate(Lane<R, H> &L, const PlaneD &pl, c
   L.t = par[5];
 #pragma unroll
   for (int e = 0; e < 21; ++e) L.cov(e) = cov[e];
-  if constexpr (sizeof(R) == sizeof(float)) legConstantsIp(L, mass, fabs(par[4]));
-  else legConstants(L, mass);
+  legConstantsIp(L, mass, fabs(par[4]));
 }
 
 // EigenStepper::update after a filter update whose predicted state is the
@@ -1082,15 +1179,29 @@ __device__ __forceinline__ void stepperUpdate(Lane<R, H> &L, const PlaneD &pl, c
 // <= 0.02: truncation below 1e-20 absolute).  The direction is scaled by
 // sin(theta_p) before its normalisation, which removes that division.  Larger
 // corrections, and directions within 1e-6 of the z axis, take stepperUpdate.
+//
+// pred and par may hold the angles as offsets from the predicted direction's
+// (absAngles == false); only their difference is used, and the rare
+// fallback restores the absolute filtered angles from the direction first.
 template <typename R, typename H>
 __device__ __forceinline__ void stepperUpdateFiltered(Lane<R, H> &L, const PlaneD &pl,
                                                       const double pred[6], const double par[6],
-                                                      const double cov[21], double mass) {
+                                                      const double cov[21], double mass,
+                                                      bool absAngles = true) {
   const double dphi = par[2] - pred[2], dth = par[3] - pred[3];
   const double dx = L.dir[0], dy = L.dir[1], dz = L.dir[2];
   const double s2 = dx * dx + dy * dy;
   if (!(fabs(dphi) <= 0.02) || !(fabs(dth) <= 0.02) || !(s2 > 1e-12)) {
-    stepperUpdate(L, pl, par, cov, mass);
+    if (absAngles) {
+      stepperUpdate(L, pl, par, cov, mass);
+    } else {
+      double full[6];
+#pragma unroll
+      for (int e = 0; e < 6; ++e) full[e] = par[e];
+      full[2] = atan2(dy, dx) + dphi;
+      full[3] = atan2(sqrt(s2), dz) + dth;
+      stepperUpdate(L, pl, full, cov, mass);
+    }
     return;
   }
 #pragma unroll
@@ -1118,8 +1229,7 @@ __device__ __forceinline__ void stepperUpdateFiltered(Lane<R, H> &L, const Plane
   L.t = par[5];
 #pragma unroll
   for (int e = 0; e < 21; ++e) L.cov(e) = cov[e];
-  if constexpr (sizeof(R) == sizeof(float)) legConstantsIp(L, mass, fabs(par[4]));
-  else legConstants(L, mass);
+  legConstantsIp(L, mass, fabs(par[4]));
 }
 
 // ---------------------------------------------------------------------------
@@ -1148,12 +1258,27 @@ static __device__ __forceinline__ bool materialStep(const Params &P, int k, cons
   return kfm::interact(P.planeSlab[k], P.materialEffects, P.planes[k].T, dir, p, q, P.mass, fx);
 }
 
+//
+// Angles of the stored states.  The smoother uses a state's angles only in
+// x_s = x_f + G (x_s' - x_p') (GainMatrixSmoother.hpp:21-94): as the
+// difference of the next state's smoothed and predicted angles, and as this
+// state's filtered angle plus a correction.  So a state after the first may
+// hold its angles as offsets from its own predicted angles (predicted 0,
+// filtered = the gain's correction, smoothed = the smoother's correction):
+// the recursion is unchanged and the first state, which keeps absolute
+// angles, comes out absolute.  The two atan2 of the predicted angles are
+// then evaluated once per track instead of once per surface.  Absolute
+// angles stay where a state's angles are read on their own: smoothed states
+// returned to the caller, the general smoother with material, the adjoint's
+// tape.
 template <typename R, typename H>
 __device__ void filterHit(Lane<R, H> &L, const Params &P, const PlaneD *planes, int k) {
   const PlaneD &pl = planes[k];
   L.hook.hitBegin(L, k);
+  constexpr bool kOffsetForm = std::is_same<H, NoHook>::value;
+  const bool absAngles = !kOffsetForm || L.measStates == 0 || P.oSmoothed != nullptr;
   double pred[6], Jst[25];
-  boundStatePlane(L, pl, pred, Jst);
+  boundStatePlane(L, pl, pred, Jst, absAngles);
   const double *mp = P.meas + (size_t)k * 5 * P.stride + L.idx;
   const double m0 = mp[0], m1 = mp[P.stride], v00 = mp[2 * P.stride],
                v01 = mp[3 * P.stride], v11 = mp[4 * P.stride];
@@ -1227,7 +1352,7 @@ __device__ void filterHit(Lane<R, H> &L, const Params &P, const PlaneD *planes, 
     if (H::kMaterial && P.materialEffects)
       for (int e = 0; e < 21; ++e) *wsCovPtr(P, L, s, 21 + e) = cf[e];
     L.chi2 += chi2;
-    stepperUpdateFiltered(L, pl, pred, filt, cf, P.mass);
+    stepperUpdateFiltered(L, pl, pred, filt, cf, P.mass, absAngles);
     if (!P.faithful) planeJacToGlobal(L, pl);
   }
   if constexpr (H::kMaterial) {

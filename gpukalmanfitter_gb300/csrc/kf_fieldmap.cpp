@@ -207,18 +207,17 @@ int32_t kf_field_map_read_xyz(const char *path, double length_unit, double field
   return 0;
 }
 
-int32_t kf_field_map_read_rz(const char *path, double length_unit, double field_unit,
-                             int32_t first_quadrant, const int32_t *n_xyz, const double *min_xyz,
-                             const double *max_xyz, kf_field_t *field, float **grid_host) {
-  if (!path || !field || !grid_host || !(length_unit > 0) || !std::isfinite(field_unit))
-    return fail(KF_ERR_INVALID_ARGUMENT, path ? path : "(null)", 0, "invalid argument");
-  *grid_host = nullptr;
-  std::vector<double> v;
+} // extern "C"
+
+namespace {
+// An (r, z) map file: its rows, and the reference's r and z axes (r never
+// mirrored, BFieldMapUtils.cpp:61-64 mirrors z only), checked for the
+// reference's point order (r slowest, z fastest).
+int32_t readRZ(const char *path, double length_unit, bool mirror, std::vector<double> &v,
+               std::vector<double> &pr, std::vector<double> &pz, Axis &ar, Axis &az) {
   if (int32_t rc = readRows(path, 4, v)) return rc;
-  const bool mirror = first_quadrant != 0;
-  // the r axis is never mirrored (BFieldMapUtils.cpp:61-64 mirrors z only)
-  Axis ar, az;
-  const std::vector<double> pr = axisPoints(v, 4, 0), pz = axisPoints(v, 4, 1);
+  pr = axisPoints(v, 4, 0);
+  pz = axisPoints(v, 4, 1);
   if (int32_t rc = makeAxis(path, pr, false, length_unit, "r", ar)) return rc;
   if (int32_t rc = makeAxis(path, pz, mirror, length_unit, "z", az)) return rc;
   const size_t rows = v.size() / 4, nr = ar.nFile, nz = az.nFile;
@@ -237,6 +236,61 @@ int32_t kf_field_map_read_rz(const char *path, double length_unit, double field_
         return fail(KF_ERR_INVALID_ARGUMENT, path, 0, m);
       }
     }
+  return 0;
+}
+} // namespace
+
+extern "C" {
+
+int32_t kf_field_map_read_rz_native(const char *path, double length_unit, double field_unit,
+                                    int32_t first_quadrant, kf_field_t *field,
+                                    float **grid_host) {
+  if (!path || !field || !grid_host || !(length_unit > 0) || !std::isfinite(field_unit))
+    return fail(KF_ERR_INVALID_ARGUMENT, path ? path : "(null)", 0, "invalid argument");
+  *grid_host = nullptr;
+  const bool mirror = first_quadrant != 0;
+  std::vector<double> v, pr, pz;
+  Axis ar, az;
+  if (int32_t rc = readRZ(path, length_unit, mirror, v, pr, pz, ar, az)) return rc;
+  const size_t nzFile = az.nFile;
+  // the reference's bins plus the zero row above the last bin on each axis:
+  // point i at lo + i * width, i = 0..nBins
+  std::memset(field, 0, sizeof(*field));
+  field->kind = KF_FIELD_GRID_RZ;
+  field->nx = ar.nBins + 1;
+  field->ny = 1;
+  field->nz = az.nBins + 1;
+  field->min[0] = ar.lo;
+  field->max[0] = ar.hi;
+  field->min[2] = az.lo;
+  field->max[2] = az.hi;
+  field->scale = 1.0;
+  const size_t nPts = (size_t)field->nx * field->nz;
+  float *g = static_cast<float *>(std::calloc(nPts * 4, sizeof(float)));
+  if (!g) return fail(KF_ERR_INVALID_ARGUMENT, path, 0, "out of host memory");
+  for (int iz = 0; iz < az.nBins; ++iz)
+    for (int ir = 0; ir < ar.nBins; ++ir) {
+      const size_t row = (size_t)ir * nzFile + fileIndex(az, iz, mirror);
+      float *o = g + 4 * ((size_t)iz * field->nx + ir);
+      o[0] = (float)(v[row * 4 + 2] * field_unit);
+      o[1] = (float)(v[row * 4 + 3] * field_unit);
+    }
+  *grid_host = g;
+  return 0;
+}
+
+int32_t kf_field_map_read_rz(const char *path, double length_unit, double field_unit,
+                             int32_t first_quadrant, const int32_t *n_xyz, const double *min_xyz,
+                             const double *max_xyz, kf_field_t *field, float **grid_host) {
+  if (!path || !field || !grid_host || !(length_unit > 0) || !std::isfinite(field_unit))
+    return fail(KF_ERR_INVALID_ARGUMENT, path ? path : "(null)", 0, "invalid argument");
+  *grid_host = nullptr;
+  std::vector<double> v, pr, pz;
+  const bool mirror = first_quadrant != 0;
+  Axis ar, az;
+  if (int32_t rc = readRZ(path, length_unit, mirror, v, pr, pz, ar, az)) return rc;
+  const size_t nr = ar.nFile, nz = az.nFile;
+  (void)nr;
   // the reference's 2D grid: bins 0..nBins-1 per axis, zero outside
   auto value = [&](int br, int bz, int c) -> double {
     if (br < 0 || br >= ar.nBins || bz < 0 || bz >= az.nBins) return 0.0;

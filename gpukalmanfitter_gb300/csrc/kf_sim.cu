@@ -45,7 +45,7 @@ extern "C" int32_t kf_simulate_tracks(const kf_synth_config_t *cfg, const double
       cfg->max_len > S || cfg->min_len > cfg->max_len)
     return kfh::fail(KF_ERR_INVALID_ARGUMENT, "kf_simulate_tracks: %s",
                      "bad track count, plane count or length range");
-  const bool useMap = field && field->kind == KF_FIELD_GRID3D;
+  const bool useMap = field && (field->kind == KF_FIELD_GRID3D || field->kind == KF_FIELD_GRID_RZ);
   const bool withMaterial = cfg->material[0] > 0. && cfg->material[3] > 0.;
   if (withMaterial && useMap)
     return kfh::fail(KF_ERR_UNSUPPORTED, "kf_simulate_tracks: %s",

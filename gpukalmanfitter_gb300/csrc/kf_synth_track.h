@@ -86,9 +86,55 @@ struct Rng {
 struct GridView {
   int n[3];
   double mn[3], mx[3], scale;
+  bool rz;           // an (r, z) grid of (br, bz) (kf_field_t kind KF_FIELD_GRID_RZ)
   const float *grid; // host or device memory, matching where the code runs;
                      // 16-byte aligned (points of 4 floats)
+  KFS_HDI float at(size_t point, int comp) const {
+#ifdef __CUDA_ARCH__
+    const float4 q = __ldg(reinterpret_cast<const float4 *>(grid) + point);
+    return comp == 0 ? q.x : comp == 1 ? q.y : q.z;
+#else
+    return grid[4 * point + comp];
+#endif
+  }
+  // bilinear in (r, z), br turned by the azimuth (fieldMapperRZ)
+  KFS_HDI void getRZ(const double p[3], double B[3]) const {
+    const double r2 = p[0] * p[0] + p[1] * p[1], r = sqrt(r2);
+    const double q[2] = {r, p[2]};
+    int idx[2];
+    double fr[2];
+    for (int a = 0; a < 2; ++a) {
+      const int ax = a == 0 ? 0 : 2;
+      const double w = (mx[ax] - mn[ax]) / (n[ax] - 1);
+      const double g = (q[a] - mn[ax]) / w;
+      int i = (int)floor(g);
+      if (i < 0) i = 0;
+      if (i > n[ax] - 2) i = n[ax] - 2;
+      idx[a] = i;
+      fr[a] = g - i;
+    }
+    const size_t nr = n[0], base = (size_t)idx[1] * nr + idx[0];
+    double v[2];
+    for (int comp = 0; comp < 2; ++comp) {
+      const double c0 = (double)at(base, comp) * (1 - fr[0]) + (double)at(base + 1, comp) * fr[0];
+      const double c1 =
+          (double)at(base + nr, comp) * (1 - fr[0]) + (double)at(base + nr + 1, comp) * fr[0];
+      v[comp] = (c0 * (1 - fr[1]) + c1 * fr[1]) * scale;
+    }
+    double cphi = 1.0, sphi = 0.0;
+    if (r2 > 2.2250738585072014e-308) {
+      cphi = p[0] / r;
+      sphi = p[1] / r;
+    }
+    B[0] = v[0] * cphi;
+    B[1] = v[0] * sphi;
+    B[2] = v[1];
+  }
   KFS_HDI void get(const double p[3], double B[3]) const {
+    if (rz) {
+      getRZ(p, B);
+      return;
+    }
     int idx[3];
     double fr[3];
     for (int a = 0; a < 3; ++a) {
@@ -137,6 +183,7 @@ KFS_HDI GridView gridView(const kf_field_t &f) {
     g.mx[a] = f.max[a];
   }
   g.scale = f.scale;
+  g.rz = f.kind == KF_FIELD_GRID_RZ;
   g.grid = f.grid;
   return g;
 }

@@ -154,7 +154,7 @@ int32_t kf_synth_tracks(const kf_synth_config_t *cfg, const double *tcenter,
   if (S <= 0 || S > KF_MAX_PLANES || cfg->min_len < 1 || cfg->max_len > S ||
       cfg->min_len > cfg->max_len)
     return KF_ERR_INVALID_ARGUMENT;
-  const bool useMap = field && field->kind == KF_FIELD_GRID3D;
+  const bool useMap = field && (field->kind == KF_FIELD_GRID3D || field->kind == KF_FIELD_GRID_RZ);
   const bool withMaterial = cfg->material[0] > 0. && cfg->material[3] > 0.;
   if (withMaterial && useMap) return KF_ERR_UNSUPPORTED; // material truth: uniform field only
   if (useMap && !field->grid) return KF_ERR_INVALID_ARGUMENT;

@@ -21,15 +21,17 @@ from . import TESLA, KfField, _check, load
 @dataclass
 class FieldMap:
     """A grid ready for kf_field_t: `grid` float32 [nz, ny, nx, 4] (host),
-    `dims` (nx, ny, nz), `min` / `max` per axis in mm."""
+    `dims` (nx, ny, nz), `min` / `max` per axis in mm, `kind` the
+    kf_field_kind (1: (x, y, z) grid; 2: (r, z) grid of (br, bz), ny = 1)."""
     grid: np.ndarray
     dims: tuple
     min: tuple
     max: tuple
+    kind: int = 1
 
     def field(self, grid_ptr: int | None = None, scale: float = 1.0) -> KfField:
         f = KfField()
-        f.kind = 1
+        f.kind = self.kind
         f.nx, f.ny, f.nz = self.dims
         for a in range(3):
             f.min[a], f.max[a] = self.min[a], self.max[a]
@@ -50,8 +52,12 @@ def _lib() -> C.CDLL:
         lib.kf_field_map_read_rz.argtypes = [C.c_char_p, C.c_double, C.c_double, C.c_int32,
                                              C.c_void_p, C.c_void_p, C.c_void_p,
                                              C.POINTER(KfField), C.POINTER(C.c_void_p)]
+        lib.kf_field_map_read_rz_native.argtypes = [C.c_char_p, C.c_double, C.c_double,
+                                                    C.c_int32, C.POINTER(KfField),
+                                                    C.POINTER(C.c_void_p)]
         lib.kf_field_map_read_xyz.restype = C.c_int32
         lib.kf_field_map_read_rz.restype = C.c_int32
+        lib.kf_field_map_read_rz_native.restype = C.c_int32
         lib.kf_field_map_free.argtypes = [C.c_void_p]
         lib.kf_field_map_free.restype = None
         lib._fieldmap_bound = True
@@ -65,7 +71,8 @@ def _take(lib, f: KfField, ptr: C.c_void_p) -> FieldMap:
         grid = np.ctypeslib.as_array(C.cast(ptr, C.POINTER(C.c_float)), shape=(n,)).copy()
     finally:
         lib.kf_field_map_free(ptr)
-    return FieldMap(grid.reshape(dims[2], dims[1], dims[0], 4), dims, tuple(f.min), tuple(f.max))
+    return FieldMap(grid.reshape(dims[2], dims[1], dims[0], 4), dims, tuple(f.min), tuple(f.max),
+                    int(f.kind))
 
 
 def read_field_map_xyz(path, length_unit: float = 1.0, field_unit: float = TESLA,
@@ -84,12 +91,19 @@ def read_field_map_xyz(path, length_unit: float = 1.0, field_unit: float = TESLA
 
 def read_field_map_rz(path, length_unit: float = 1.0, field_unit: float = TESLA,
                       first_quadrant: bool = False, n_xyz=None, min_xyz=None,
-                      max_xyz=None) -> FieldMap:
-    """An RZ map ("r z br bz", r slowest) resampled onto a Cartesian grid
-    (default: x, y over +-r_max at the r step, z over the map's range)."""
+                      max_xyz=None, native: bool = True) -> FieldMap:
+    """An RZ map ("r z br bz", r slowest).  native (default): the (r, z) grid
+    the fit interpolates in (r, z) as the reference does
+    (kf_field_map_read_rz_native); native=False: resampled onto a Cartesian
+    grid (default: x, y over +-r_max at the r step, z over the map's range)."""
     lib = _lib()
     f = KfField()
     ptr = C.c_void_p()
+    if native and n_xyz is None:
+        _check(lib.kf_field_map_read_rz_native(os.fsencode(os.fspath(path)), length_unit,
+                                               field_unit, int(first_quadrant), C.byref(f),
+                                               C.byref(ptr)))
+        return _take(lib, f, ptr)
     args = [None, None, None]
     keep = []
     if n_xyz is not None:

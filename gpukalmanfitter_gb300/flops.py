@@ -24,7 +24,7 @@ RK_STEP = 591      # field map: accepted step: time, transport matrix blocks, D*
 # uniform field: the step through c = d x B, e = c x B (kfa::polyPrep/polyCoef/polyAcceptFwd)
 POLY_TRIAL = 24    # trial coefficients and error estimate
 POLY_STEP = 354    # c, e (23) + motion, k4, D blocks (173) + D*J (139) + path (1) + navigation (18)
-FILTER = 950       # boundState to a plane (J C J^T on the non-zeros) + gain update + reload
+FILTER = 936       # boundState to a plane (J C J^T on the non-zeros) + gain update + reload
 SMOOTH = 367       # one RTS smoother state: structured J^-1 (gain), state, Pg <- G Pg
 FIXED = 1270       # start state on the perigee line, C_s(0) = Pg C Pg^T, final transport
 

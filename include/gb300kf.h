@@ -77,7 +77,13 @@ enum kf_precision {
   KF_PRECISION_MIXED = 1 /* FP32 RK4/field/transport, FP64 gain/update/smoother */
 };
 
-enum kf_field_kind { KF_FIELD_CONSTANT = 0, KF_FIELD_GRID3D = 1 };
+enum kf_field_kind {
+  KF_FIELD_CONSTANT = 0, /* Test::ConstantBField (Test/Helper.hpp:17-22) */
+  KF_FIELD_GRID3D = 1,   /* trilinear on an (x, y, z) grid (fieldMapperXYZ) */
+  KF_FIELD_GRID_RZ = 2   /* bilinear on an (r, z) grid of (br, bz), rotated by the
+                            position's azimuth (fieldMapperRZ,
+                            src/MagneticField/BFieldMapUtils.cpp:17-136) */
+};
 
 enum kf_kernel_kind {
   KF_KERNEL_AUTO = 0,
@@ -150,12 +156,17 @@ typedef struct kf_geometry {
  * (MagneticField/InterpolatedBFieldMap.hpp:87-208). */
 typedef struct kf_field {
   int32_t kind;             /* kf_field_kind */
-  int32_t nx, ny, nz;       /* grid points per axis (grid only) */
+  int32_t nx, ny, nz;       /* grid points per axis (grid only); (r, z) grid:
+                               nx points in r, ny = 1, nz points in z */
   double value[3];          /* constant field (constant only) */
   double scale;             /* global multiplier applied to every lookup */
-  double min[3], max[3];    /* grid extent in mm: point i at min + i*(max-min)/(n-1) */
+  double min[3], max[3];    /* grid extent in mm: point i at min + i*(max-min)/(n-1);
+                               (r, z) grid: r over min[0]..max[0], z over
+                               min[2]..max[2] */
   const float *grid;        /* DEVICE [nz][ny][nx][4] = (bx, by, bz, 0) in
-                               GeV/(e*mm); index ((iz*ny)+iy)*nx+ix */
+                               GeV/(e*mm); index ((iz*ny)+iy)*nx+ix.  (r, z)
+                               grid: [nz][nx][4] = (br, bz, 0, 0), index
+                               iz*nx+ir */
 } kf_field_t;
 
 /* Per-track inputs (structure of arrays). */

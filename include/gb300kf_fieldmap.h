@@ -61,6 +61,17 @@ int32_t kf_field_map_read_rz(const char *path, double length_unit, double field_
                              int32_t first_quadrant, const int32_t *n_xyz, const double *min_xyz,
                              const double *max_xyz, kf_field_t *field, float **grid_host);
 
+/* An (r, z) map as the reference interpolates it: the grid of the file's
+ * (br, bz) points plus the zero row above the last point on each axis
+ * (kind KF_FIELD_GRID_RZ, nx = r points, ny = 1, nz = z points), looked up
+ * bilinearly in (r, z) at r = |(x, y)| and rotated by the position's azimuth,
+ * (br cos phi, br sin phi, bz) with phi = 0 on the axis (fieldMapperRZ,
+ * BFieldMapUtils.cpp:17-136).  Same file format and checks as
+ * kf_field_map_read_rz; first_quadrant mirrors z. */
+int32_t kf_field_map_read_rz_native(const char *path, double length_unit, double field_unit,
+                                    int32_t first_quadrant, kf_field_t *field,
+                                    float **grid_host);
+
 void kf_field_map_free(float *grid_host);
 
 #ifdef __cplusplus

@@ -73,6 +73,7 @@ def load(variant: str = "default"):
         lib.kf_synth_field_map.restype = C.c_int32
         lib.kf_synth_field_map.argtypes = [C.c_double, C.c_int32, C.c_double, C.c_void_p]
         lib.kf_synth_tracks.restype = C.c_int32
+        lib.oracle_field_value.restype = C.c_int32
         _LIBS[variant] = lib
     return _LIBS[variant]
 
@@ -129,6 +130,19 @@ class Fitter:
         if self.st is not None:
             self.out["states"] = self.st
         return self.out
+
+
+def field_value(field, pos) -> np.ndarray:
+    """One lookup of a kf_field_t (grid in host memory) as the oracle's fit
+    makes it."""
+    lib = load()
+    out = np.zeros(3)
+    p = np.ascontiguousarray(pos, dtype=np.float64)
+    rc = lib.oracle_field_value(C.byref(field), p.ctypes.data_as(C.POINTER(C.c_double)),
+                                out.ctypes.data_as(C.POINTER(C.c_double)))
+    if rc != 0:
+        raise RuntimeError(f"oracle_field_value returned {rc}")
+    return out
 
 
 def fit(tel, cfg=None, *, threads: int = 0, smoothed: bool = False, masks: bool = True,

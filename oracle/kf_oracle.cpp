@@ -29,6 +29,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <limits>
 #include <cstring>
 #include <vector>
 
@@ -385,6 +386,7 @@ struct Field {
   V3 get(const V3 &p) const {
     if (kind == KF_FIELD_CONSTANT)
       return v3(value[0] * scale, value[1] * scale, value[2] * scale);
+    if (kind == KF_FIELD_GRID_RZ) return getRZ(p);
     int idx[3];
     double f[3];
     for (int a = 0; a < 3; ++a) {
@@ -411,6 +413,45 @@ struct Field {
       out[comp] = (c0 * (1 - f[2]) + c1 * f[2]) * scale;
     }
     return v3(out[0], out[1], out[2]);
+  }
+  // An (r, z) map (src/MagneticField/BFieldMapUtils.cpp:17-136): the
+  // position goes to (perp(pos), z) (transformPos, :97-99), the grid of
+  // (br, bz) is interpolated in its cell (in r, then in z; positions outside
+  // the grid use the boundary cell), and (br, bz) goes back to
+  // (br cos phi, br sin phi, bz) with cos phi = x / r, sin phi = y / r, or
+  // phi = 0 on the axis (transformBField, :103-116).
+  V3 getRZ(const V3 &p) const {
+    const double r2 = p[0] * p[0] + p[1] * p[1];
+    const double q[2] = {std::sqrt(r2), p[2]};
+    const int ax[2] = {0, 2};
+    int idx[2];
+    double f[2];
+    for (int a = 0; a < 2; ++a) {
+      const int k = ax[a];
+      const double w = (mx[k] - mn[k]) / (n[k] - 1);
+      const double g = (q[a] - mn[k]) / w;
+      int i = (int)std::floor(g);
+      i = std::min(std::max(i, 0), n[k] - 2);
+      idx[a] = i;
+      f[a] = g - i;
+    }
+    double v[2];
+    for (int comp = 0; comp < 2; ++comp) {
+      auto at = [&](int dr, int dz) {
+        const size_t k = (size_t)(idx[1] + dz) * n[0] + (idx[0] + dr);
+        return (double)grid[4 * k + comp];
+      };
+      const double c0 = at(0, 0) * (1 - f[0]) + at(1, 0) * f[0];
+      const double c1 = at(0, 1) * (1 - f[0]) + at(1, 1) * f[0];
+      v[comp] = (c0 * (1 - f[1]) + c1 * f[1]) * scale;
+    }
+    double cphi = 1., sphi = 0.;
+    if (r2 > std::numeric_limits<double>::min()) {
+      const double inv = 1. / std::sqrt(r2);
+      cphi = p[0] * inv;
+      sphi = p[1] * inv;
+    }
+    return v3(v[0] * cphi, v[0] * sphi, v[1]);
   }
 };
 
@@ -1468,6 +1509,27 @@ void oracle_config_default(kf_config_t *c) {
   c->faithful_jacobian = 1;
   c->kernel = KF_KERNEL_AUTO;
   c->block_size = 0;
+}
+
+// one field lookup as the fit makes it (Field::get); the grid is host memory
+int32_t oracle_field_value(const kf_field_t *field, const double pos[3], double out[3]) {
+  using namespace kfo;
+  if (!field || !pos || !out) return KF_ERR_INVALID_ARGUMENT;
+  Field B;
+  B.kind = field->kind;
+  B.scale = field->scale;
+  for (int a = 0; a < 3; ++a) {
+    B.value[a] = field->value[a];
+    B.mn[a] = field->min[a];
+    B.mx[a] = field->max[a];
+  }
+  B.n[0] = field->nx;
+  B.n[1] = field->ny;
+  B.n[2] = field->nz;
+  B.grid = field->grid;
+  const V3 b = B.get(v3(pos[0], pos[1], pos[2]));
+  for (int a = 0; a < 3; ++a) out[a] = b[a];
+  return KF_SUCCESS;
 }
 
 int32_t oracle_num_threads(void) {

@@ -96,7 +96,7 @@ def test_rz_map(tmp_path):
     br = -0.5 * R * bz * (-2 * Z / 3000.0 ** 2)
     p = tmp_path / "rz.txt"
     FM.write_field_map_rz(p, r, z, np.stack([br, bz], axis=-1), fmt="%.17g")
-    fm = FM.read_field_map_rz(p)
+    fm = FM.read_field_map_rz(p, native=False)
     ref = OF.MapRZ(p, field_unit=TESLA)
     assert fm.dims == (31, 31, 21)
     assert np.allclose(fm.min, (-1500., -1500., -2000.)) and np.allclose(fm.max, (1500., 1500., 2000.))
@@ -114,7 +114,7 @@ def test_rz_map(tmp_path):
     assert c[1] == 0.0
     # a chosen Cartesian grid
     fm2 = FM.read_field_map_rz(p, n_xyz=(5, 5, 5), min_xyz=(-100., -100., -100.),
-                               max_xyz=(100., 100., 100.))
+                               max_xyz=(100., 100., 100.), native=False)
     assert fm2.dims == (5, 5, 5)
     assert np.max(np.abs(fm2.grid[4, 4, 4, :3] - ref.field([100., 100., 100.]))) <= 1e-7 * bmax
     # mirrored quadrant
@@ -123,13 +123,99 @@ def test_rz_map(tmp_path):
     q = tmp_path / "quadrant.txt"
     FM.write_field_map_rz(q, r, half, np.stack([R2 * 0 + 0.1, 2 - Z2 / 2000.], axis=-1),
                           fmt="%.17g")
-    fq = FM.read_field_map_rz(q, first_quadrant=True)
+    fq = FM.read_field_map_rz(q, first_quadrant=True, native=False)
     refq = OF.MapRZ(q, field_unit=TESLA, first_quadrant=True)
     assert fq.dims[2] == 21 and np.isclose(fq.min[2], -2000.)
     pos = [300., -400., -1234.]
     a = OF.trilinear(fq.grid, fq.dims, fq.min, fq.max, pos)
     # bz is linear in z, so only br's direction interpolation differs
     assert abs(a[2] - refq.field(pos)[2]) <= 1e-6 * abs(refq.field(pos)[2])
+
+
+def _rz_test_map(path, r_step=100.0, z_step=200.0):
+    """the analytic telescope map's (br, bz) on an (r, z) grid, as an RZ file
+    in tesla"""
+    r = np.arange(0., 1500. + r_step / 2, r_step)
+    z = np.arange(-2000., 2000. + z_step / 2, z_step)
+    R, Z = np.meshgrid(r, z, indexing="ij")
+    bz = 2.0 * (1 - 0.2 * R ** 2 / 1500.0 ** 2) * np.exp(-(Z / 3000.0) ** 2)
+    br = R * Z / 3000.0 ** 2 * bz
+    FM.write_field_map_rz(path, r, z, np.stack([br, bz], axis=-1), fmt="%.17g")
+    return r, z
+
+
+def test_rz_native_map(orc, tmp_path):
+    """The native (r, z) grid: the file's points plus the zero row above the
+    last point on each axis; the oracle's lookup in it (the fit's) equals the
+    reference's RZ interpolation restated in numpy (float32 grid values) over
+    the whole range including the fall to zero, on the axis and with a
+    mirrored quadrant; and the Cartesian resampling differs from it by the
+    O(h^2 B'') of trilinear interpolation."""
+    from oracle import field_map as OF
+    p = tmp_path / "rz.txt"
+    r, z = _rz_test_map(p)
+    fm = FM.read_field_map_rz(p)
+    assert fm.kind == 2 and fm.dims == (len(r) + 1, 1, len(z) + 1)
+    assert np.allclose(fm.min, (0., 0., -2000.)) and np.allclose(fm.max, (1600., 0., 2200.))
+    ref = OF.MapRZ(p, field_unit=TESLA)
+    for ir in range(len(r)):
+        for iz in range(len(z)):
+            assert np.array_equal(fm.grid[iz, 0, ir, :2], ref.bin_value(ir, iz).astype(np.float32))
+    assert np.all(fm.grid[-1] == 0) and np.all(fm.grid[:, :, -1] == 0)
+    f = fm.field()
+    bmax = np.abs(fm.grid).max()
+    rng = np.random.default_rng(3)
+    for _ in range(400):
+        rr, ph, zz = rng.uniform(0, 1590.), rng.uniform(-np.pi, np.pi), rng.uniform(-1990., 2190.)
+        pos = [rr * np.cos(ph), rr * np.sin(ph), zz]
+        assert np.max(np.abs(orc.field_value(f, pos) - ref.field(pos))) <= 1e-7 * bmax
+    on_axis = orc.field_value(f, [0., 0., 333.])
+    assert on_axis[1] == 0.0 and np.allclose(on_axis, ref.field([0., 0., 333.]), atol=1e-7 * bmax)
+    # mirrored quadrant
+    q = tmp_path / "quadrant.txt"
+    half = np.linspace(0., 2000., 11)
+    R2, Z2 = np.meshgrid(r, half, indexing="ij")
+    FM.write_field_map_rz(q, r, half, np.stack([0.1 + R2 * 0, 2 - Z2 / 2000.], axis=-1),
+                          fmt="%.17g")
+    fq = FM.read_field_map_rz(q, first_quadrant=True)
+    refq = OF.MapRZ(q, field_unit=TESLA, first_quadrant=True)
+    assert fq.dims[2] == 22 and np.isclose(fq.min[2], -2000.)
+    for pos in ([300., -400., -1234.], [-20., 5., 1999.], [1000., 1000., -5.]):
+        assert np.allclose(orc.field_value(fq.field(), pos), refq.field(pos), atol=1e-7 * bmax)
+    # the Cartesian resampling at the r step: trilinear between its points
+    fc = FM.read_field_map_rz(p, native=False)
+    dev = 0.0
+    for _ in range(400):
+        pos = rng.uniform([-1000., -1000., -1900.], [1000., 1000., 1900.])
+        dev = max(dev, float(np.max(np.abs(orc.field_value(fc.field(), pos) - ref.field(pos)))))
+    assert 1e-6 * bmax < dev < 2e-2 * bmax, dev
+
+
+@pytest.mark.gpu
+def test_gpu_fit_in_native_rz_map(kf, orc, tmp_path):
+    """Tracks simulated and fitted in a native (r, z) map: the FP64 plain and
+    batched forms against the precise oracle at 1e-9, the mixed form at its
+    accuracy bar."""
+    p = tmp_path / "rz.txt"
+    _rz_test_map(p, r_step=50.0, z_step=50.0)
+    fm = FM.read_field_map_rz(p)
+    tel = kf.make_telescope(3000, seed=24, field_map=fm, n_planes=10)
+    cfg = kf.default_config(overstep_limit=0.1)
+    o = orc.fit(tel, cfg, threads=0, variant="precise")
+    assert np.mean(o["status"] == 0) > 0.99
+    from conftest import parity_report
+    for form in ("grid", "batched"):
+        b = kf.DeviceBatch(tel, cfg)
+        b.fit() if form == "grid" else b.fit_sorted()
+        g = b.results()
+        assert np.array_equal(g["status"], o["status"]) and np.array_equal(g["n_steps"], o["n_steps"])
+        rep = parity_report(g, o, 1e-9, mask=o["status"] == 0)
+        assert rep["params"] <= 1.0 and rep["chi2"] <= 1.0 and rep["cov"] <= 1.0, (form, rep)
+    g = kf.fit_device(tel, kf.default_config(overstep_limit=0.1, precision=1))
+    ok = (g["status"] == 0) & (o["status"] == 0)
+    sig = np.sqrt(np.abs(o["cov"][[0, 6, 11, 15, 18, 20]]))[:, ok]
+    rel = np.abs(g["params"][:, ok] - o["params"][:, ok]) / np.maximum(np.abs(o["params"][:, ok]), sig)
+    assert np.all(np.median(rel, axis=1) <= 1e-6), np.median(rel, axis=1)
 
 
 def test_malformed_files(tmp_path):
