@@ -72,7 +72,7 @@ struct Params {
   int nSurf;
   int maxSteps, maxTrials, smoothing, faithful;
   double tol, cutoff, mass, overstep, surfTol, outlierCut;
-  float tolLoF, tolHiF; // mixed form: FP32 accept/reject band around tol
+  float tolLoF, tolHiF; // mixed form: FP32 acceptance below tolLoF, else the FP64 trial decides
   const double *meas;
   const uint64_t *mask;
   const int32_t *nplanes;
@@ -120,7 +120,7 @@ enum { PC_PRE = 0, PC_LOOP = 1, PC_ACT = 2, PC_POST = 3, PC_DONE = 4 };
 // (br, bz) grid interpolated bilinearly at r = |(x, y)| (in r, then in z), and
 // br turned by the position's azimuth (cos phi = x / r, sin phi = y / r; phi =
 // 0 on the axis, the reference's transformBField)
-static __device__ __noinline__ void getFieldRZ(const FieldD &F, const double p[3], double B[3]) {
+static __device__ __forceinline__ void getFieldRZ(const FieldD &F, const double p[3], double B[3]) {
   const double r2 = p[0] * p[0] + p[1] * p[1];
   const double r = sqrt(r2);
   const double gr = (r - F.mn[0]) * F.invw[0], gz = (p[2] - F.mn[2]) * F.invw[2];
@@ -293,12 +293,12 @@ __device__ __forceinline__ void getFieldFF(const FieldD &F, const float at[3],
 // dynamic shared memory, one column per thread ([element][thread]: a warp's
 // 32 lanes touch 32 consecutive words, no bank conflicts), so that the
 // stepping loop's register set stays small.  Layout for a CTA of n threads:
-// cov [21][n] double, then g03 [12][n] and g46 [6][n] in R.
+// cov [21][n], then g03 [12][n] and g46 [6][n], all double.
 // ---------------------------------------------------------------------------
 constexpr int kLaneSlots = 128; // threads per CTA of the grid form and the adjoint
 extern __shared__ __align__(16) unsigned char kfColdSmem[];
 template <typename R> __host__ __device__ constexpr size_t coldStateBytes(int threads = kLaneSlots) {
-  return (size_t)threads * (21 * sizeof(double) + 18 * sizeof(R));
+  return (size_t)threads * (21 + 18) * sizeof(double);
 }
 
 // Recording hook of a lane: the fit kernels use NoHook (every call compiles
@@ -328,18 +328,24 @@ template <typename R, typename H = NoHook> struct Lane {
   double ss[4]; // ConstrainedStep values
   int ssDir;    // ConstrainedStep direction (+1 / -1)
   int navDir;
-  R JA[3][3], Ja[3], Jb, JB[3][3], Jc[3]; // transport Jacobian blocks
+  // transport Jacobian blocks.  Plain form: the blocks themselves.  Mixed
+  // form: JA and JB hold their offsets from the straight line's, JA - sTr I
+  // and JB - I, with sTr the path since the last reset in FP64, so that
+  // their FP32 rounding scales with the field's bending, not with the blocks
+  // (see applyTransportOffsets and boundStatePlaneMixed).
+  R JA[3][3], Ja[3], Jb, JB[3][3], Jc[3];
+  double sTr;   // path since the last Jacobian reset (mixed form)
   R k4[3];     // k4 of the last step (derivative rows 4..6)
   bool stepped; // a step since the last Jacobian reset (else derivative = 0)
   // cold state (shared memory, see coldStateBytes)
   __device__ __forceinline__ double &cov(int e) const {
     return reinterpret_cast<double *>(kfColdSmem)[e * blockDim.x + threadIdx.x];
   }
-  __device__ __forceinline__ R &g03(int r, int c) const {
-    return reinterpret_cast<R *>(kfColdSmem + 21 * sizeof(double) * blockDim.x)[(r * 4 + c) * blockDim.x + threadIdx.x];
+  __device__ __forceinline__ double &g03(int r, int c) const {
+    return reinterpret_cast<double *>(kfColdSmem + 21 * sizeof(double) * blockDim.x)[(r * 4 + c) * blockDim.x + threadIdx.x];
   }
-  __device__ __forceinline__ R &g46(int r, int c) const {
-    return reinterpret_cast<R *>(kfColdSmem + (21 * sizeof(double) + 12 * sizeof(R)) * blockDim.x)
+  __device__ __forceinline__ double &g46(int r, int c) const {
+    return reinterpret_cast<double *>(kfColdSmem + 33 * sizeof(double) * blockDim.x)
         [(r * 2 + c) * blockDim.x + threadIdx.x];
   }
   // per-leg constants (functions of p only)
@@ -445,17 +451,20 @@ template <typename R, typename H> __device__ __forceinline__ void legConstants(L
 
 // ---- Jacobian resets -------------------------------------------------------
 template <typename R, typename H> __device__ __forceinline__ void resetTransport(Lane<R, H> &L) {
+  // the mixed form's JB holds JB - I
+  constexpr R one = sizeof(R) == sizeof(float) ? R(0) : R(1);
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
       L.JA[i][j] = R(0);
-      L.JB[i][j] = (i == j) ? R(1) : R(0);
+      L.JB[i][j] = (i == j) ? one : R(0);
     }
     L.Ja[i] = R(0);
     L.Jc[i] = R(0);
   }
   L.Jb = R(0);
+  L.sTr = 0.;
   L.stepped = false;
 }
 
@@ -476,27 +485,50 @@ template <typename R, typename H> __device__ __forceinline__ DirTrig<R> dirTrig(
   t.sinP = y * t.invS;
   return t;
 }
-
-// PlaneSurface::initJacobianToGlobal (PlaneSurface.ipp:122-156)
+// FP64 in both forms.  The mixed form takes 1 / sin(theta) from an FP32
+// estimate refined by two Newton steps (rsqrtNewton, sin^2 theta is near 1
+// on a telescope and bounded away from 0 wherever the bound frame exists)
+// instead of the FP64 square root and division.
 template <typename R, typename H>
-__device__ __forceinline__ void planeJacToGlobal(Lane<R, H> &L, const PlaneD &pl, const DirTrig<R> &tr) {
-  const R cosT = tr.cosT, sinT = tr.sinT, cosP = tr.cosP, sinP = tr.sinP;
+__device__ __forceinline__ DirTrig<double> dirTrigD(const Lane<R, H> &L) {
+  DirTrig<double> t;
+  const double x = L.dir[0], y = L.dir[1], z = L.dir[2];
+  const double s2 = x * x + y * y;
+  t.cosT = z;
+  if constexpr (sizeof(R) == sizeof(float)) {
+    t.invS = rsqrtNewton(s2);
+    t.sinT = s2 * t.invS;
+  } else {
+    t.sinT = sqrt(s2);
+    t.invS = 1. / t.sinT;
+  }
+  t.cosP = x * t.invS;
+  t.sinP = y * t.invS;
+  return t;
+}
+
+// PlaneSurface::initJacobianToGlobal (PlaneSurface.ipp:122-156), in FP64 in
+// both forms
+template <typename R, typename H>
+__device__ __forceinline__ void planeJacToGlobal(Lane<R, H> &L, const PlaneD &pl,
+                                                 const DirTrig<double> &tr) {
+  const double cosT = tr.cosT, sinT = tr.sinT, cosP = tr.cosP, sinP = tr.sinP;
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
-    L.g03(r, 0) = (R)pl.U[r];
-    L.g03(r, 1) = (R)pl.V[r];
-    L.g03(r, 2) = R(0);
-    L.g03(r, 3) = R(0);
+    L.g03(r, 0) = pl.U[r];
+    L.g03(r, 1) = pl.V[r];
+    L.g03(r, 2) = 0.;
+    L.g03(r, 3) = 0.;
   }
   L.g46(0, 0) = (-sinT) * sinP;
   L.g46(0, 1) = cosT * cosP;
   L.g46(1, 0) = sinT * cosP;
   L.g46(1, 1) = cosT * sinP;
-  L.g46(2, 0) = R(0);
+  L.g46(2, 0) = 0.;
   L.g46(2, 1) = (-sinT);
 }
 template <typename R, typename H> __device__ __forceinline__ void planeJacToGlobal(Lane<R, H> &L, const PlaneD &pl) {
-  planeJacToGlobal(L, pl, dirTrig(L));
+  planeJacToGlobal(L, pl, dirTrigD(L));
 }
 
 // LineSurface::referenceFrame (LineSurface.ipp:46-61), line axis z
@@ -655,6 +687,41 @@ template <typename R, typename H>
 __device__ __forceinline__ void applyTransportStep(Lane<R, H> &L, const R DA[3][3], const R DB[3][3],
                                                    const R Da[3], const R Dc[3], R D37);
 
+// The mixed form's J = D J on offsets from the straight line: with
+// A = s I + dA, B = I + dB (the lane's JA, JB), DA = h I + dDA, DB = I + dDB,
+//   dA' = dA + h dB + dDA (I + dB),  a' = a + h c + dDA c + Da,
+//   dB' = dB + dDB (I + dB),         c' = c + dDB c + Dc,   b' = b + D37,
+// every FP32 term a field-induced quantity (the path s is advanced in FP64).
+template <typename R, typename H>
+__device__ __forceinline__ void applyTransportOffsets(Lane<R, H> &L, R h, const R dDA[3][3],
+                                                      const R dDB[3][3], const R Da[3],
+                                                      const R Dc[3], R D37) {
+  R nA[3][3], na[3], nB[3][3], nc[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const R pA = dDA[i][j] + dDA[i][0] * L.JB[0][j] + dDA[i][1] * L.JB[1][j] + dDA[i][2] * L.JB[2][j];
+      const R pB = dDB[i][j] + dDB[i][0] * L.JB[0][j] + dDB[i][1] * L.JB[1][j] + dDB[i][2] * L.JB[2][j];
+      nA[i][j] = L.JA[i][j] + (h * L.JB[i][j] + pA);
+      nB[i][j] = L.JB[i][j] + pB;
+    }
+    na[i] = L.Ja[i] + (h * L.Jc[i] + (dDA[i][0] * L.Jc[0] + dDA[i][1] * L.Jc[1] + dDA[i][2] * L.Jc[2] + Da[i]));
+    nc[i] = L.Jc[i] + (dDB[i][0] * L.Jc[0] + dDB[i][1] * L.Jc[1] + dDB[i][2] * L.Jc[2] + Dc[i]);
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      L.JA[i][j] = nA[i][j];
+      L.JB[i][j] = nB[i][j];
+    }
+    L.Ja[i] = na[i];
+    L.Jc[i] = nc[i];
+  }
+  L.Jb = L.Jb + D37;
+}
+
 // transportMatrix (EigenStepper.ipp:50-124) on its non-zero blocks and
 // jacTransport = D * jacTransport (EigenStepper.ipp:312-318)
 template <typename R, typename H>
@@ -708,21 +775,25 @@ __device__ __forceinline__ void transportUpdate(Lane<R, H> &L, const R dir[3], R
   nextT(T1, half_h, s.Bm, T2);
   nextT(T2, half_h, s.Bm, T3);
   nextT(T3, h, s.Bl, T4);
-  // D blocks: dFdT (A), dGdT (I + Bd), dFdL (a), dGdL (c), D(3,7)
+  // D blocks: dFdT (A), dGdT (I + Bd), dFdL (a), dGdL (c), D(3,7).  The
+  // mixed form keeps the offsets DA - h I and DB - I (applyTransportOffsets).
+  constexpr bool kOffsets = sizeof(R) == sizeof(float);
+  const R one = kOffsets ? R(0) : R(1);
   R DA[3][3], DB[3][3], Da[3], Dc[3];
   const R h6 = h / R(6);
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-      R v = ((i == j) ? R(1) : R(0)) + h6 * (T1[i][j] + T2[i][j] + T3[i][j]);
+      R v = ((i == j) ? one : R(0)) + h6 * (T1[i][j] + T2[i][j] + T3[i][j]);
       DA[i][j] = v * h;
-      DB[i][j] = ((i == j) ? R(1) : R(0)) + h6 * (T1[i][j] + R(2) * (T2[i][j] + T3[i][j]) + T4[i][j]);
+      DB[i][j] = ((i == j) ? one : R(0)) + h6 * (T1[i][j] + R(2) * (T2[i][j] + T3[i][j]) + T4[i][j]);
     }
     Da[i] = (h * h) / R(6) * (dk1dL[i] + dk2dL[i] + dk3dL[i]);
     Dc[i] = h6 * (dk1dL[i] + R(2) * (dk2dL[i] + dk3dL[i]) + dk4dL[i]);
   }
-  applyTransportStep(L, DA, DB, Da, Dc, h * d37);
+  if constexpr (kOffsets) applyTransportOffsets(L, h, DA, DB, Da, Dc, h * d37);
+  else applyTransportStep(L, DA, DB, Da, Dc, h * d37);
 }
 
 // new J = D * J on the structured blocks (EigenStepper.ipp:312-318)
@@ -844,7 +915,7 @@ template <typename R, typename H> __device__ void rkStep(Lane<R, H> &L, const Pa
     const float res[3] = {(float)(L.pos[0] - (double)posf[0]), (float)(L.pos[1] - (double)posf[1]),
                           (float)(L.pos[2] - (double)posf[2])};
     const float dirf[3] = {(float)L.dir[0], (float)L.dir[1], (float)L.dir[2]};
-    const float tolLo = P.tolLoF, tolHi = P.tolHiF;
+    const float tolLo = P.tolLoF;
     StagesDelta S;
     rkFirstDelta(P.field, posf, res, L.dir, L.qop, S);
     for (;;) {
@@ -854,10 +925,14 @@ template <typename R, typename H> __device__ void rkStep(Lane<R, H> &L, const Pa
       bool accept;
       if (errf <= tolLo) {
         accept = true;
-      } else if (errf > tolHi) {
-        accept = false;
       } else {
-        // undecided in FP32: the FP64 trial decides
+        // undecided or rejected in FP32: the FP64 trial decides and gives
+        // the error estimate that scales the next step.  The FP32 estimate
+        // is a sum of cancelling offsets, off by up to ~1e-3; the step size
+        // it sets stays the accuracy constraint for the following steps, so
+        // it would move every later accuracy-limited step off the FP64
+        // fit's (about half a rejected trial per track on the telescope
+        // workloads)
         RkStages<double> sd;
         rkFirst<double>(P.field, L.pos, L.dir, L.qop, sd);
         err = rkTrial<double>(P.field, L.pos, L.dir, L.qop, h, sd);
@@ -875,6 +950,7 @@ template <typename R, typename H> __device__ void rkStep(Lane<R, H> &L, const Pa
     }
     L.t += h * L.dtds;
     transportUpdate<float>(L, dirf, qopf, (float)h, (float)L.d37, S.s);
+    L.sTr += h;
     // motion: FP64 state, FP64 k1, FP32 sums of the offsets
     //   pos += h d + h^2/6 (3 k1 + d2 + d3),  dir += h/6 (6 k1 + 2 (d2 + d3) + d4)
     const double hh6 = h * h * (1. / 6.), h6 = h * (1. / 6.);
@@ -916,16 +992,19 @@ template <typename R> struct Transported {
 
 template <typename R, typename H>
 __device__ __forceinline__ void applyTransport(const Lane<R, H> &L, Transported<R> &X) {
+  // mixed form: JA = sTr I + dA, JB = I + dB (applyTransportOffsets)
+  constexpr bool kOffsets = sizeof(R) == sizeof(float);
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
-    X.Pt[r][0] = L.g03(r, 0);
-    X.Pt[r][1] = L.g03(r, 1);
+    X.Pt[r][0] = (R)L.g03(r, 0);
+    X.Pt[r][1] = (R)L.g03(r, 1);
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
-      X.Pt[r][2 + c] = L.g03(r, 2 + c) + L.JA[r][0] * L.g46(0, c) +
-                       L.JA[r][1] * L.g46(1, c) + L.JA[r][2] * L.g46(2, c);
-      X.Dd[r][2 + c] = L.JB[r][0] * L.g46(0, c) + L.JB[r][1] * L.g46(1, c) +
-                       L.JB[r][2] * L.g46(2, c);
+      const R g0 = (R)L.g46(0, c), g1 = (R)L.g46(1, c), g2 = (R)L.g46(2, c);
+      const R gr = (R)L.g46(r, c);
+      X.Pt[r][2 + c] = (kOffsets ? (R)(L.g03(r, 2 + c) + L.sTr * L.g46(r, c)) : (R)L.g03(r, 2 + c)) +
+                       L.JA[r][0] * g0 + L.JA[r][1] * g1 + L.JA[r][2] * g2;
+      X.Dd[r][2 + c] = (kOffsets ? gr : R(0)) + L.JB[r][0] * g0 + L.JB[r][1] * g1 + L.JB[r][2] * g2;
     }
     X.Pt[r][4] = L.Ja[r];
     X.Dd[r][0] = R(0);
@@ -943,9 +1022,9 @@ __device__ __forceinline__ void applyTransport(const Lane<R, H> &L, Transported<
 // and cov <- J cov J^T (in FP64).  ax0/ax1 are the surface's local axes
 // (rows 0 and 1 of jacToLocal); the direction rows follow
 // PlaneSurface.ipp:158-189 / LineSurface.ipp:114-143.
-template <typename R, typename H>
+template <typename R, typename H, typename TR>
 __device__ __forceinline__ void projectCov(Lane<R, H> &L, Transported<R> &X, const R sVec[5],
-                                           const R ax0[3], const R ax1[3], const DirTrig<R> &tr,
+                                           const R ax0[3], const R ax1[3], const DirTrig<TR> &tr,
                                            double Jst[25]) {
   // derivative (EigenStepper.ipp:320-325): direction, dt/ds and k4 of the
   // last step; zero right after a Jacobian reset
@@ -965,7 +1044,8 @@ __device__ __forceinline__ void projectCov(Lane<R, H> &L, Transported<R> &X, con
     }
     X.R3[c] -= der[3] * sVec[c];
   }
-  const R cosT = tr.cosT, sinT = tr.sinT, invS = tr.invS, cosP = tr.cosP, sinP = tr.sinP;
+  const R cosT = (R)tr.cosT, sinT = (R)tr.sinT, invS = (R)tr.invS, cosP = (R)tr.cosP,
+          sinP = (R)tr.sinP;
   const R j24 = -sinP * invS, j25 = cosP * invS;
   const R j34 = cosP * cosT, j35 = sinP * cosT, j36 = -sinT;
   // the Jacobian's arithmetic type: FP32 in the mixed form (Jacobian
@@ -1082,10 +1162,217 @@ __device__ __forceinline__ void boundAngles(const Lane<R, H> &L, double out[6], 
   out[5] = L.t;
 }
 
+// 1 / a from an FP32 estimate and two Newton steps y <- y (2 - a y) (each
+// squares the relative error), for a of moderate magnitude
+__device__ __forceinline__ double rcpNewton(double a) {
+  double y = (double)(1.f / (float)a);
+  y = y * (2. - a * y);
+  return y * (2. - a * y);
+}
+
+// C <- J C J^T in FP64 with the bound-to-bound Jacobian J (rows 0-3 and 5,
+// columns 0-4; row 4 is e4 and column 5 is e5), on the structural non-zeros,
+// and J stored for the smoother (mixed form; projectCov does the same for
+// the plain form)
+template <typename R, typename H>
+__device__ __forceinline__ void transportCovD(Lane<R, H> &L, const double J[6][5], double Jst[25]) {
+  double M[4][5];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+      double v = J[i][0] * L.cov(sidx(0, j));
+#pragma unroll
+      for (int k = 1; k < 5; ++k) v += J[i][k] * L.cov(sidx(k, j));
+      M[i][j] = v;
+    }
+  }
+  // time: N = C J(5, :)^T with J(5, 5) = 1, C'(i, 5) = J(i, :) N
+  double N[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    double v = L.cov(sidx(k, 5));
+#pragma unroll
+    for (int l = 0; l < 5; ++l) v += L.cov(sidx(k, l)) * J[5][l];
+    N[k] = v;
+  }
+  double T5[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    if (i == 4) {
+      T5[4] = N[4];
+    } else {
+      double v = (i == 5) ? N[5] : 0.;
+#pragma unroll
+      for (int k = 0; k < 5; ++k) v += J[i][k] * N[k];
+      T5[i] = v;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+#pragma unroll
+    for (int j = i; j < 5; ++j) {
+      double v;
+      if (i == 4) {
+        v = L.cov(ut(4, 4));
+      } else if (j == 4) {
+        v = M[i][4];
+      } else {
+        v = M[i][0] * J[j][0];
+#pragma unroll
+        for (int k = 1; k < 5; ++k) v += M[i][k] * J[j][k];
+      }
+      L.cov(ut(i, j)) = v;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 6; ++i) L.cov(ut(i, 5)) = T5[i];
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    Jst[c] = J[0][c];
+    Jst[5 + c] = J[1][c];
+    Jst[10 + c] = J[2][c];
+    Jst[15 + c] = J[3][c];
+    Jst[20 + c] = J[5][c];
+  }
+}
+
+// boundState<PlaneSurface> in the mixed form (CovarianceEngine.hpp:269-290,
+// :106-125; PlaneSurface.ipp:158-204), as the straight line's bound
+// Jacobian plus the field-induced remainder.  With JA = s I + dA, JB = I + dB
+// the transported jacToGlobal splits into (G03 + s G46, G46), which with
+// the derivative term of the direction and the plane's projections gives
+// the O(1) entries of J in FP64, and the blocks dA G46, dB G46, Ja, Jc with
+// the k4 and dt/ds derivative terms, field-induced, in FP32.  J comes out
+// accurate to FP32 rounding of those small terms (an FP32 J moves the fitted
+// perigee by up to 3e-6 of its resolution on the 30-plane map telescope,
+// mostly through the angle rows), and the covariance transport and the
+// smoother take it in FP64.
+template <typename H>
+__device__ void boundStatePlaneMixed(Lane<float, H> &L, const PlaneD &pl, double out[6],
+                                     double Jst[25], bool absAngles) {
+  const DirTrig<double> td = dirTrigD(L);
+  const double s = L.sTr;
+  const bool st = L.stepped;
+  // ---- straight-line part, FP64
+  const double dp = pl.T[0] * L.dir[0] + pl.T[1] * L.dir[1] + pl.T[2] * L.dir[2];
+  const double idp = rcpNewton(dp);
+  const double nv[3] = {pl.T[0] * idp, pl.T[1] * idp, pl.T[2] * idp};
+  double P0[3][4], s0[4];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) P0[r][c] = L.g03(r, c) + (c >= 2 ? s * L.g46(r, c - 2) : 0.);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) s0[c] = nv[0] * P0[0][c] + nv[1] * P0[1][c] + nv[2] * P0[2][c];
+  if (st) {
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) P0[r][c] -= L.dir[r] * s0[c];
+  }
+  const double j24 = -td.sinP * td.invS, j25 = td.cosP * td.invS;
+  const double j34 = td.cosP * td.cosT, j35 = td.sinP * td.cosT, j36 = -td.sinT;
+  double J[6][5];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    J[0][c] = pl.U[0] * P0[0][c] + pl.U[1] * P0[1][c] + pl.U[2] * P0[2][c];
+    J[1][c] = pl.V[0] * P0[0][c] + pl.V[1] * P0[1][c] + pl.V[2] * P0[2][c];
+    if (c >= 2) {
+      const double g0 = L.g46(0, c - 2), g1 = L.g46(1, c - 2), g2 = L.g46(2, c - 2);
+      J[2][c] = j24 * g0 + j25 * g1;
+      J[3][c] = j34 * g0 + j35 * g1 + j36 * g2;
+    } else {
+      J[2][c] = 0.;
+      J[3][c] = 0.;
+    }
+  }
+  // ---- field-induced part, FP32
+  float G[3][2];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    G[r][0] = (float)L.g46(r, 0);
+    G[r][1] = (float)L.g46(r, 1);
+  }
+  float dP[3][5], dD[3][5];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    dP[r][0] = dP[r][1] = dD[r][0] = dD[r][1] = 0.f;
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      dP[r][2 + c] = L.JA[r][0] * G[0][c] + L.JA[r][1] * G[1][c] + L.JA[r][2] * G[2][c];
+      dD[r][2 + c] = L.JB[r][0] * G[0][c] + L.JB[r][1] * G[1][c] + L.JB[r][2] * G[2][c];
+    }
+    dP[r][4] = L.Ja[r];
+    dD[r][4] = L.Jc[r];
+  }
+  const float nvf[3] = {(float)nv[0], (float)nv[1], (float)nv[2]};
+  float ds[5], sf[5];
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    ds[c] = nvf[0] * dP[0][c] + nvf[1] * dP[1][c] + nvf[2] * dP[2][c];
+    sf[c] = (c < 4 ? (float)s0[c] : 0.f) + ds[c];
+  }
+  float R3[5];
+  if (st) {
+    const float d0 = (float)L.dir[0], d1 = (float)L.dir[1], d2 = (float)L.dir[2];
+    const float dt = (float)L.dtds;
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      dP[0][c] -= d0 * ds[c];
+      dP[1][c] -= d1 * ds[c];
+      dP[2][c] -= d2 * ds[c];
+      dD[0][c] -= L.k4[0] * sf[c];
+      dD[1][c] -= L.k4[1] * sf[c];
+      dD[2][c] -= L.k4[2] * sf[c];
+      R3[c] = (c == 4 ? L.Jb : 0.f) - dt * sf[c];
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < 5; ++c) R3[c] = (c == 4 ? L.Jb : 0.f);
+  }
+  const float U[3] = {(float)pl.U[0], (float)pl.U[1], (float)pl.U[2]};
+  const float V[3] = {(float)pl.V[0], (float)pl.V[1], (float)pl.V[2]};
+  const float f24 = (float)j24, f25 = (float)j25, f34 = (float)j34, f35 = (float)j35, f36 = (float)j36;
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    const float e0 = U[0] * dP[0][c] + U[1] * dP[1][c] + U[2] * dP[2][c];
+    const float e1 = V[0] * dP[0][c] + V[1] * dP[1][c] + V[2] * dP[2][c];
+    const float e2 = f24 * dD[0][c] + f25 * dD[1][c];
+    const float e3 = f34 * dD[0][c] + f35 * dD[1][c] + f36 * dD[2][c];
+    if (c < 4) {
+      J[0][c] += (double)e0;
+      J[1][c] += (double)e1;
+      J[2][c] += (double)e2;
+      J[3][c] += (double)e3;
+    } else {
+      J[0][4] = (double)e0;
+      J[1][4] = (double)e1;
+      J[2][4] = (double)e2;
+      J[3][4] = (double)e3;
+    }
+    J[4][c] = (c == 4) ? 1. : 0.;
+    J[5][c] = (double)R3[c];
+  }
+  transportCovD(L, J, Jst);
+  // reinitializeJacobians (CovarianceEngine.hpp:169-201)
+  resetTransport(L);
+  planeJacToGlobal(L, pl, td);
+  const double d0 = L.pos[0] - pl.c[0], d1 = L.pos[1] - pl.c[1], d2 = L.pos[2] - pl.c[2];
+  out[0] = pl.U[0] * d0 + pl.U[1] * d1 + pl.U[2] * d2;
+  out[1] = pl.V[0] * d0 + pl.V[1] * d1 + pl.V[2] * d2;
+  double mom[3];
+  boundAngles(L, out, mom, absAngles);
+}
+
 // boundState<PlaneSurface> (EigenStepper.ipp:516-540) incl. re-initialisation
 template <typename R, typename H>
 __device__ void boundStatePlane(Lane<R, H> &L, const PlaneD &pl, double out[6], double Jst[25],
                                 bool absAngles = true) {
+  if constexpr (sizeof(R) == sizeof(float)) {
+    boundStatePlaneMixed(L, pl, out, Jst, absAngles);
+    return;
+  }
   Transported<R> X;
   applyTransport(L, X);
   // PlaneSurface::derivativeFactors (PlaneSurface.ipp:191-204)
@@ -1098,7 +1385,7 @@ __device__ void boundStatePlane(Lane<R, H> &L, const PlaneD &pl, double out[6], 
   for (int c = 0; c < 5; ++c) sVec[c] = nv0 * X.Pt[0][c] + nv1 * X.Pt[1][c] + nv2 * X.Pt[2][c];
   const R U[3] = {(R)pl.U[0], (R)pl.U[1], (R)pl.U[2]};
   const R V[3] = {(R)pl.V[0], (R)pl.V[1], (R)pl.V[2]};
-  const DirTrig<R> tr = dirTrig(L);
+  const DirTrig<double> tr = dirTrigD(L);
   projectCov(L, X, sVec, U, V, tr, Jst);
   // reinitializeJacobians (CovarianceEngine.hpp:169-201)
   resetTransport(L);
