@@ -18,7 +18,8 @@
 //      segment again through the same lane program while a hook records a
 //      tape (step pre-states and trial step sizes, step-size constraint
 //      updates, surface events), then sweep the tape backwards with the
-//      vector-Jacobian products of kf_adjoint_math.h.
+//      vector-Jacobian products of kf_adjoint_math.h.  The last two segments
+//      are taped by the forward itself and are not recomputed.
 // The step size is part of the differentiated function: an accepted step's
 // size carries its adjoint to the constraint that set it (the distance to the
 // next plane, or the accuracy step of an earlier rejected trial, which in
@@ -39,6 +40,8 @@ namespace adj {
 
 constexpr int kEvery = 5;          // measurement states per checkpointed segment
 constexpr int kTapeWords = 3072;   // tape capacity per track and segment (doubles)
+constexpr int kForwardTaped = 2;   // last segments the forward tapes (not recomputed)
+constexpr int kTapeCap = kForwardTaped * kTapeWords; // tape capacity per track
 constexpr int kSnapWords = 128;    // doubles per lane checkpoint (visitLane writes 115)
 enum { REC_STEP = 1, REC_ACT = 2, REC_HIT = 3 };
 constexpr int kStepFixed = 33;     // pos 3, dir 3, t, p, transport Jacobian 25
@@ -49,7 +52,7 @@ struct AdjParams {
   double *xs;        // [S][6][n] smoothed parameters (by position)
   int32_t *info;     // [S][n] plane index | outlier << 8 (by position)
   double *snap;      // [nCk][kSnapWords][n] (by position)
-  double *tape;      // [kTapeWords][n] (by position: a warp's lanes at the same tape
+  double *tape;      // [kTapeCap][n] (by position: a warp's lanes at the same tape
                      // offset touch one contiguous line)
   double *alignPart; // [S][6][n] (by track)
   double *trackFs;   // [n] per-track d chi2 / d field scale (by track)
@@ -79,7 +82,7 @@ struct TapeHook {
   bool rec, full;
 
   __device__ __forceinline__ void put(double v) {
-    if (top < kTapeWords) tape[(int64_t)top * n] = v;
+    if (top < kTapeCap) tape[(int64_t)top * n] = v;
     else full = true;
     ++top;
   }
@@ -254,9 +257,12 @@ template <class V> __device__ void visitLane(ALane &L, V &v) {
     }
 }
 
-// first measurement state of a lane's last checkpoint segment
+// first measurement state of the segments the forward tapes: the last
+// kForwardTaped checkpoint segments of the lane
 __device__ __forceinline__ int lastSegmentStart(const ALane &L) {
-  return L.nHits > 0 ? (L.nHits - 1) / kEvery * kEvery : 0;
+  if (L.nHits <= 0) return 0;
+  const int first = (L.nHits - 1) / kEvery - (kForwardTaped - 1);
+  return first > 0 ? first * kEvery : 0;
 }
 
 __device__ __forceinline__ bool hitPending(const ALane &L) {
@@ -269,8 +275,8 @@ __device__ __forceinline__ bool hitPending(const ALane &L) {
 // (stopAt < 0: never).  As in the fit kernel, lanes step independently and
 // run their surface events together once every lane waits.  With ck (the
 // forward of a gradient run), a lane saves itself before the hit events of
-// states 5, 10, ... and records the tape of its last segment as it runs it:
-// the reverse sweep starts there without recomputing it.
+// states 5, 10, ... and records the tape of its last kForwardTaped segments
+// as it runs them: the reverse sweep starts there without recomputing them.
 __device__ void runWarp(ALane &L, const Params &P, const PlaneD *sp, const AdjParams &A,
                         int stopAt, bool ck) {
   bool stopped = false;
@@ -655,7 +661,7 @@ __global__ void __launch_bounds__(kLaneSlots, KF_ADJ_MIN_BLOCKS)
   L.hook.rec = false;
   L.hook.full = false;
   if (valid) zeroTrack(P, A, i);
-  // ---- A: forward fit with checkpoints (and the last segment's tape)
+  // ---- A: forward fit with checkpoints (and the last segments' tape)
   initLane(L, P, sp, valid ? i : -1, valid ? u : 0);
   L.hook.rec = valid && A.grad != 0 && lastSegmentStart(L) == 0;
   runWarp(L, P, sp, A, -1, A.grad != 0);
@@ -674,7 +680,10 @@ __global__ void __launch_bounds__(kLaneSlots, KF_ADJ_MIN_BLOCKS)
   bool failed = false;
   for (int c = maxSeg - 1; c >= 0; --c) {
     const bool act = ok && !failed && c < nseg;
-    const bool taped = act && c == nseg - 1; // recorded by the forward
+    // the forward recorded the last kForwardTaped segments: the first of
+    // them swept (c == nseg - 1) takes the whole forward tape
+    const bool taped = act && c >= nseg - kForwardTaped;
+    const bool sweepTape = !taped || c == nseg - 1;
     if (!taped) L.hook.top = 0;
     L.hook.rec = act && !taped;
     if (!act || taped) {
@@ -688,7 +697,7 @@ __global__ void __launch_bounds__(kLaneSlots, KF_ADJ_MIN_BLOCKS)
     }
     runWarp(L, P, sp, A, (c + 1) * kEvery, false);
     if (act && L.hook.full) failed = true;
-    const bool sweep = act && !failed;
+    const bool sweep = act && !failed && sweepTape;
     if (!reverseWarp(TapeRef{L.hook.tape, P.n}, sweep ? L.hook.top : 0, R, P, sp, A, u, i, q) &&
         sweep)
       failed = true;
@@ -752,7 +761,7 @@ AdjLayout adjLayout(int64_t n, int32_t S) {
   L.xs = take((size_t)S * 6 * n * 8);
   L.info = take((size_t)S * n * 4);
   L.snap = take((size_t)(nCk > 0 ? nCk : 1) * kSnapWords * n * 8);
-  L.tape = take((size_t)kTapeWords * n * 8);
+  L.tape = take((size_t)kTapeCap * n * 8);
   L.alignPart = take((size_t)S * 6 * n * 8);
   L.trackFs = take((size_t)n * 8);
   L.perm = take((size_t)n * 4);

@@ -72,7 +72,7 @@ struct Params {
   int nSurf;
   int maxSteps, maxTrials, smoothing, faithful;
   double tol, cutoff, mass, overstep, surfTol, outlierCut;
-  float tolLoF, tolHiF; // mixed form: FP32 acceptance below tolLoF, else the FP64 trial decides
+  float tolLoF, tolHiF; // mixed form: FP32 accept/reject band around tol
   const double *meas;
   const uint64_t *mask;
   const int32_t *nplanes;
@@ -915,7 +915,7 @@ template <typename R, typename H> __device__ void rkStep(Lane<R, H> &L, const Pa
     const float res[3] = {(float)(L.pos[0] - (double)posf[0]), (float)(L.pos[1] - (double)posf[1]),
                           (float)(L.pos[2] - (double)posf[2])};
     const float dirf[3] = {(float)L.dir[0], (float)L.dir[1], (float)L.dir[2]};
-    const float tolLo = P.tolLoF;
+    const float tolLo = P.tolLoF, tolHi = P.tolHiF;
     StagesDelta S;
     rkFirstDelta(P.field, posf, res, L.dir, L.qop, S);
     for (;;) {
@@ -925,14 +925,10 @@ template <typename R, typename H> __device__ void rkStep(Lane<R, H> &L, const Pa
       bool accept;
       if (errf <= tolLo) {
         accept = true;
+      } else if (errf > tolHi) {
+        accept = false;
       } else {
-        // undecided or rejected in FP32: the FP64 trial decides and gives
-        // the error estimate that scales the next step.  The FP32 estimate
-        // is a sum of cancelling offsets, off by up to ~1e-3; the step size
-        // it sets stays the accuracy constraint for the following steps, so
-        // it would move every later accuracy-limited step off the FP64
-        // fit's (about half a rejected trial per track on the telescope
-        // workloads)
+        // undecided in FP32: the FP64 trial decides
         RkStages<double> sd;
         rkFirst<double>(P.field, L.pos, L.dir, L.qop, sd);
         err = rkTrial<double>(P.field, L.pos, L.dir, L.qop, h, sd);

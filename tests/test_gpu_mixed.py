@@ -1,7 +1,10 @@
-"""The mixed-precision form (FP32 field interpolation, RK stages and
-Jacobians; FP64 state, covariance transport, gain, Joseph update and smoother
-correction) against the FP64 oracle: same control flow on almost every
-track, median parameter error at most 1e-6 relative, pull widths within 1 %."""
+"""The mixed-precision form (FP32 field interpolation, RK stages and the
+field-induced parts of the Jacobians; FP64 state, straight-line Jacobian,
+covariance transport, gain, Joseph update and smoother correction) against
+the FP64 oracle: same control flow on almost every track, parameter error
+at most 1e-6 relative (scale max(|x|, sigma)) on 99 % of the tracks and
+2e-6 on 99.9 % of them, the largest deviation reported, pull widths within
+1 %."""
 import numpy as np
 import pytest
 
@@ -34,8 +37,9 @@ def test_mixed_against_fp64_oracle(kf, orc, workload):
     med = np.median(rel, axis=1)
     p99 = np.percentile(rel, 99, axis=1)
     print("median", med, "p99", p99, "max", rel.max(axis=1))
-    assert np.all(med <= 1e-6), med
-    assert np.all(p99 <= 2e-5), p99
+    assert np.all(med <= 1e-7), med
+    assert np.all(p99 <= 1e-6), p99
+    assert np.all(rel.max(axis=1) <= 2e-5), rel.max(axis=1)
     wg, wo = _pull_widths(g, tel, ok), _pull_widths(o, tel, ok)
     assert np.all(np.abs(wg / wo - 1) < 0.01), (wg, wo)
 
@@ -50,7 +54,8 @@ def test_mixed_holes_outliers(kf, orc):
     assert np.mean(g["status"] == o["status"]) >= 0.999
     assert np.mean(g["n_meas"] == o["n_meas"]) >= 0.999
     ok, rel = _errors(g, o)
-    assert np.all(np.median(rel, axis=1) <= 1e-6), np.median(rel, axis=1)
+    assert np.all(np.median(rel, axis=1) <= 1e-7), np.median(rel, axis=1)
+    assert np.all(np.percentile(rel, 99, axis=1) <= 1e-6), np.percentile(rel, 99, axis=1)
 
 
 NAMES = ["d0", "z0", "phi", "theta", "qop", "t"]
@@ -77,11 +82,18 @@ def test_config3_1M_map30_accuracy(kf, orc):
              for k, nm in enumerate(NAMES)}
     c2 = np.abs(g["chi2"][ok] - o["chi2"][ok]) / np.maximum(o["chi2"][ok], 1e-300)
     wg, wo = _pull_widths(g, tel, ok), _pull_widths(o, tel, ok)
+    above = float(np.mean(rel.max(axis=0) > 1e-6))
     print("mixed vs FP64, 1M map30:", stats)
+    print("tracks with a parameter beyond 1e-6:", above)
     print("chi2 rel: median", np.median(c2), "p99", np.percentile(c2, 99), "max", c2.max())
     print("pull widths mixed", wg, "fp64", wo)
     med = np.array([stats[nm]["median"] for nm in NAMES])
     p99 = np.array([stats[nm]["p99"] for nm in NAMES])
-    assert np.all(med <= 1e-6), stats
-    assert np.all(p99 <= 2e-5), stats
+    p999 = np.array([stats[nm]["p99.9"] for nm in NAMES])
+    mx = np.array([stats[nm]["max"] for nm in NAMES])
+    assert np.all(med <= 1e-7), stats
+    assert np.all(p99 <= 1e-6), stats
+    assert np.all(p999 <= 2e-6), stats
+    assert np.all(mx <= 2e-5), stats
+    assert above < 0.005, above
     assert np.all(np.abs(wg / wo - 1) < 0.01), (wg, wo)
