@@ -45,7 +45,7 @@ class KfConfig(C.Structure):
                 ("on_surface_tol", C.c_double), ("outlier_chi2_cut", C.c_double),
                 ("faithful_jacobian", C.c_int32), ("kernel", C.c_int32),
                 ("block_size", C.c_int32), ("min_blocks_per_sm", C.c_int32),
-                ("material_effects", C.c_int32), ("reserved0", C.c_int32)]
+                ("material_effects", C.c_int32), ("adjoint_tape", C.c_int32)]
 
 
 class KfGeometry(C.Structure):

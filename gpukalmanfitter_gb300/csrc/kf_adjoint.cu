@@ -39,9 +39,14 @@ namespace kfd {
 namespace adj {
 
 constexpr int kEvery = 5;          // measurement states per checkpointed segment
-constexpr int kTapeWords = 3072;   // tape capacity per track and segment (doubles)
-constexpr int kForwardTaped = 2;   // last segments the forward tapes (not recomputed)
-constexpr int kTapeCap = kForwardTaped * kTapeWords; // tape capacity per track
+constexpr int kTapeSegment = 3072; // least tape capacity per track: one recomputed segment (doubles)
+constexpr int kTapePerState = 256; // tape capacity per track and surface for the forward's tape
+// tape capacity per track: the forward's tape of a whole track of S surfaces
+// (the workload of 20 planes uses at most ~210 words a state), and never less
+// than one segment for a lane that recomputes
+__host__ __device__ constexpr int tapeWords(int S) {
+  return S * kTapePerState > kTapeSegment ? S * kTapePerState : kTapeSegment;
+}
 constexpr int kSnapWords = 128;    // doubles per lane checkpoint (visitLane writes 115)
 enum { REC_STEP = 1, REC_ACT = 2, REC_HIT = 3 };
 constexpr int kStepFixed = 33;     // pos 3, dir 3, t, p, transport Jacobian 25
@@ -52,8 +57,10 @@ struct AdjParams {
   double *xs;        // [S][6][n] smoothed parameters (by position)
   int32_t *info;     // [S][n] plane index | outlier << 8 (by position)
   double *snap;      // [nCk][kSnapWords][n] (by position)
-  double *tape;      // [kTapeCap][n] (by position: a warp's lanes at the same tape
+  double *tape;      // [tapeCap][n] (by position: a warp's lanes at the same tape
                      // offset touch one contiguous line)
+  int tapeCap;       // tape words per track
+  int fwdTape;       // the forward records the whole track's tape
   double *alignPart; // [S][6][n] (by track)
   double *trackFs;   // [n] per-track d chi2 / d field scale (by track)
   double *chi2;      // [n]
@@ -78,12 +85,12 @@ struct TapeHook {
   double *tape; // this lane's word 0; word k at tape[k * n]
   int32_t *info;
   int64_t n;
-  int top, head, state, plane;
-  bool rec, full;
+  int top, head, state, plane, cap;
+  bool rec, full, over; // recording; a step failed; the tape ran over its capacity
 
   __device__ __forceinline__ void put(double v) {
-    if (top < kTapeCap) tape[(int64_t)top * n] = v;
-    else full = true;
+    if (top < cap) tape[(int64_t)top * n] = v;
+    else over = true;
     ++top;
   }
   template <class LT> __device__ __forceinline__ void putJ(const LT &L) {
@@ -257,14 +264,6 @@ template <class V> __device__ void visitLane(ALane &L, V &v) {
     }
 }
 
-// first measurement state of the segments the forward tapes: the last
-// kForwardTaped checkpoint segments of the lane
-__device__ __forceinline__ int lastSegmentStart(const ALane &L) {
-  if (L.nHits <= 0) return 0;
-  const int first = (L.nHits - 1) / kEvery - (kForwardTaped - 1);
-  return first > 0 ? first * kEvery : 0;
-}
-
 __device__ __forceinline__ bool hitPending(const ALane &L) {
   return L.parked && L.current >= 0 && !L.smoothed && !L.finished &&
          ((L.mask >> L.current) & 1ull);
@@ -275,8 +274,8 @@ __device__ __forceinline__ bool hitPending(const ALane &L) {
 // (stopAt < 0: never).  As in the fit kernel, lanes step independently and
 // run their surface events together once every lane waits.  With ck (the
 // forward of a gradient run), a lane saves itself before the hit events of
-// states 5, 10, ... and records the tape of its last kForwardTaped segments
-// as it runs them: the reverse sweep starts there without recomputing them.
+// states 5, 10, ...: a lane whose tape ran over its capacity recomputes its
+// segments from there.
 __device__ void runWarp(ALane &L, const Params &P, const PlaneD *sp, const AdjParams &A,
                         int stopAt, bool ck) {
   bool stopped = false;
@@ -289,10 +288,6 @@ __device__ void runWarp(ALane &L, const Params &P, const PlaneD *sp, const AdjPa
         if (ck && hitPending(L) && L.measStates > 0 && L.measStates % kEvery == 0) {
           Saver s{A.snap + (int64_t)(L.measStates / kEvery - 1) * kSnapWords * P.n + L.wsIdx, P.n, 0};
           visitLane(L, s);
-          if (L.measStates == lastSegmentStart(L)) {
-            L.hook.top = 0;
-            L.hook.rec = true;
-          }
         }
         runEvent(L, P, sp);
       }
@@ -658,12 +653,14 @@ __global__ void __launch_bounds__(kLaneSlots, KF_ADJ_MIN_BLOCKS)
   L.hook.info = A.info + (valid ? u : 0);
   L.hook.n = P.n;
   L.hook.top = L.hook.head = L.hook.state = L.hook.plane = 0;
+  L.hook.cap = A.tapeCap;
   L.hook.rec = false;
-  L.hook.full = false;
+  L.hook.full = L.hook.over = false;
   if (valid) zeroTrack(P, A, i);
-  // ---- A: forward fit with checkpoints (and the last segments' tape)
+  // ---- A: forward fit with checkpoints and the tape (recording from before
+  // initLane, which already sets the step constraint towards the first plane)
+  L.hook.rec = valid && A.grad != 0 && A.fwdTape != 0;
   initLane(L, P, sp, valid ? i : -1, valid ? u : 0);
-  L.hook.rec = valid && A.grad != 0 && lastSegmentStart(L) == 0;
   runWarp(L, P, sp, A, -1, A.grad != 0);
   const int ns = L.measStates;
   const bool ok = valid && L.status == KF_TRACK_OK && ns > 0;
@@ -671,35 +668,40 @@ __global__ void __launch_bounds__(kLaneSlots, KF_ADJ_MIN_BLOCKS)
   // ---- B: smoothed chi2 (and the smoother's adjoints)
   if (ok) A.chi2[i] = smoothChi2(P, A, u, i, ns, A.grad != 0);
   if (!A.grad) return;
-  // ---- C: segments, last first, all lanes together
+  // ---- C: the reverse sweep.  A lane whose forward tape holds the whole
+  // track sweeps it in one pass (at its last segment's turn); a lane whose
+  // tape ran over recomputes its segments from the checkpoints, last first,
+  // each onto the start of its tape, and sweeps them one by one.
   Adj R;
   adjZero(R);
   const double q = L.q;
   const int nseg = ok ? (ns - 1) / kEvery + 1 : 0;
   const int maxSeg = __reduce_max_sync(0xffffffffu, nseg);
-  bool failed = false;
+  const bool fwdTaped = A.fwdTape && !L.hook.over;
+  const int fwdTop = L.hook.top;
+  bool failed = ok && L.hook.full;
   for (int c = maxSeg - 1; c >= 0; --c) {
     const bool act = ok && !failed && c < nseg;
-    // the forward recorded the last kForwardTaped segments: the first of
-    // them swept (c == nseg - 1) takes the whole forward tape
-    const bool taped = act && c >= nseg - kForwardTaped;
-    const bool sweepTape = !taped || c == nseg - 1;
-    if (!taped) L.hook.top = 0;
-    L.hook.rec = act && !taped;
-    if (!act || taped) {
+    const bool recompute = act && !fwdTaped;
+    L.hook.rec = recompute;
+    if (!recompute) {
       L.pc = PC_DONE;
       L.parked = false;
-    } else if (c == 0) {
-      initLane(L, P, sp, i, u);
     } else {
-      Loader ld{A.snap + (int64_t)(c - 1) * kSnapWords * P.n + u, P.n, 0};
-      visitLane(L, ld);
+      L.hook.top = 0;
+      L.hook.over = false;
+      if (c == 0) {
+        initLane(L, P, sp, i, u);
+      } else {
+        Loader ld{A.snap + (int64_t)(c - 1) * kSnapWords * P.n + u, P.n, 0};
+        visitLane(L, ld);
+      }
     }
     runWarp(L, P, sp, A, (c + 1) * kEvery, false);
-    if (act && L.hook.full) failed = true;
-    const bool sweep = act && !failed && sweepTape;
-    if (!reverseWarp(TapeRef{L.hook.tape, P.n}, sweep ? L.hook.top : 0, R, P, sp, A, u, i, q) &&
-        sweep)
+    if (recompute && (L.hook.full || L.hook.over)) failed = true;
+    const bool sweep = act && !failed && (recompute || c == nseg - 1);
+    const int top = recompute ? L.hook.top : fwdTop;
+    if (!reverseWarp(TapeRef{L.hook.tape, P.n}, sweep ? top : 0, R, P, sp, A, u, i, q) && sweep)
       failed = true;
   }
   if (!ok) return;
@@ -747,7 +749,10 @@ size_t alignUp(size_t x) { return (x + 255) & ~(size_t)255; }
 struct AdjLayout {
   size_t ws, stateBar, xs, info, snap, tape, alignPart, trackFs, perm, hist, offs, total;
 };
-AdjLayout adjLayout(int64_t n, int32_t S) {
+// tape words per track for kf_config_t.adjoint_tape
+int tapeCapacity(int mode, int32_t S) { return mode == 1 ? kTapeSegment : tapeWords(S); }
+
+AdjLayout adjLayout(int64_t n, int32_t S, int mode) {
   AdjLayout L{};
   size_t o = 0;
   auto take = [&](size_t b) {
@@ -761,7 +766,7 @@ AdjLayout adjLayout(int64_t n, int32_t S) {
   L.xs = take((size_t)S * 6 * n * 8);
   L.info = take((size_t)S * n * 4);
   L.snap = take((size_t)(nCk > 0 ? nCk : 1) * kSnapWords * n * 8);
-  L.tape = take((size_t)kTapeCap * n * 8);
+  L.tape = take((size_t)tapeCapacity(mode, S) * n * 8);
   L.alignPart = take((size_t)S * 6 * n * 8);
   L.trackFs = take((size_t)n * 8);
   L.perm = take((size_t)n * 4);
@@ -780,9 +785,8 @@ using namespace kfd::adj;
 extern "C" {
 
 size_t kf_adjoint_workspace_size(const kf_config_t *cfg, int64_t n_tracks, int32_t n_surfaces) {
-  (void)cfg;
   if (n_tracks <= 0 || n_surfaces <= 0) return 0;
-  return adjLayout(n_tracks, n_surfaces).total;
+  return adjLayout(n_tracks, n_surfaces, cfg ? cfg->adjoint_tape : 0).total;
 }
 
 int32_t kf_adjoint_batch(const kf_inputs_t *in, kf_adjoint_outputs_t *out, const kf_config_t *cfg,
@@ -802,6 +806,8 @@ int32_t kf_adjoint_batch(const kf_inputs_t *in, kf_adjoint_outputs_t *out, const
     return fail(KF_ERR_UNSUPPORTED, "the adjoint follows faithful_jacobian = 1 only%s");
   if (cfg->material_effects && geo->material)
     return fail(KF_ERR_UNSUPPORTED, "the adjoint has no material effects%s");
+  if (cfg->adjoint_tape != 0 && cfg->adjoint_tape != 1)
+    return fail(KF_ERR_INVALID_ARGUMENT, "adjoint_tape must be 0 or 1%s");
   const int64_t n = in->n_tracks;
   const int32_t S = in->n_surfaces;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -814,7 +820,7 @@ int32_t kf_adjoint_batch(const kf_inputs_t *in, kf_adjoint_outputs_t *out, const
   }
   if (!in->meas || !in->start_params || !in->start_cov || !in->perigee)
     return fail(KF_ERR_INVALID_ARGUMENT, "missing input array%s");
-  const AdjLayout L = adjLayout(n, S);
+  const AdjLayout L = adjLayout(n, S, cfg->adjoint_tape);
   if (!workspace || workspace_bytes < L.total)
     return fail(KF_ERR_WORKSPACE_TOO_SMALL, "workspace smaller than kf_adjoint_workspace_size()%s");
   char *base = static_cast<char *>(workspace);
@@ -832,6 +838,8 @@ int32_t kf_adjoint_batch(const kf_inputs_t *in, kf_adjoint_outputs_t *out, const
   A.info = reinterpret_cast<int32_t *>(base + L.info);
   A.snap = reinterpret_cast<double *>(base + L.snap);
   A.tape = reinterpret_cast<double *>(base + L.tape);
+  A.tapeCap = tapeCapacity(cfg->adjoint_tape, S);
+  A.fwdTape = cfg->adjoint_tape == 0;
   A.alignPart = reinterpret_cast<double *>(base + L.alignPart);
   A.trackFs = (compute_gradient && out->grad_field_scale_track)
                   ? out->grad_field_scale_track

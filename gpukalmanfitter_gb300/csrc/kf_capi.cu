@@ -135,7 +135,6 @@ void fillParams(Params &P, const kf_inputs_t *in, const kf_outputs_t *out, const
   F.scalef = (float)F.scale;
   F.scalelo = (float)(F.scale - (double)F.scalef);
   P.tolLoF = (float)(P.tol * 0.99);
-  P.tolHiF = (float)(P.tol * 1.01);
   for (int k = 0; k < in->n_surfaces; ++k) {
     PlaneD &pl = P.planes[k];
     for (int r = 0; r < 3; ++r) {

@@ -72,7 +72,7 @@ struct Params {
   int nSurf;
   int maxSteps, maxTrials, smoothing, faithful;
   double tol, cutoff, mass, overstep, surfTol, outlierCut;
-  float tolLoF, tolHiF; // mixed form: FP32 accept/reject band around tol
+  float tolLoF;         // mixed form: FP32 error estimates up to this accept
   const double *meas;
   const uint64_t *mask;
   const int32_t *nplanes;
@@ -915,26 +915,24 @@ template <typename R, typename H> __device__ void rkStep(Lane<R, H> &L, const Pa
     const float res[3] = {(float)(L.pos[0] - (double)posf[0]), (float)(L.pos[1] - (double)posf[1]),
                           (float)(L.pos[2] - (double)posf[2])};
     const float dirf[3] = {(float)L.dir[0], (float)L.dir[1], (float)L.dir[2]};
-    const float tolLo = P.tolLoF, tolHi = P.tolHiF;
+    const float tolLo = P.tolLoF;
     StagesDelta S;
     rkFirstDelta(P.field, posf, res, L.dir, L.qop, S);
     for (;;) {
       L.rkTrials++;
       const float errf = rkTrialDelta(P.field, posf, res, dirf, qopf, (float)h, S);
-      double err = errf;
-      bool accept;
-      if (errf <= tolLo) {
-        accept = true;
-      } else if (errf > tolHi) {
-        accept = false;
-      } else {
-        // undecided in FP32: the FP64 trial decides
-        RkStages<double> sd;
-        rkFirst<double>(P.field, L.pos, L.dir, L.qop, sd);
-        err = rkTrial<double>(P.field, L.pos, L.dir, L.qop, h, sd);
-        accept = err <= P.tol;
-      }
-      if (accept) break;
+      if (errf <= tolLo) break;
+      // Not clearly accepted: the FP64 trial decides, and a rejection sets
+      // the next trial's size from its error estimate.  The FP32 estimate is
+      // a sum of offsets that cancel to ~1 % of their size, good to ~1e-5
+      // relative: rescaled from it, the step sizes (the RK partition of the
+      // path) would drift from the FP64 fit's by ~3e-6, and a later decision
+      // near the tolerance can then go the other way (1e-4 of the perigee's
+      // resolution on a few tracks in 1e6).
+      RkStages<double> sd;
+      rkFirst<double>(P.field, L.pos, L.dir, L.qop, sd);
+      const double err = rkTrial<double>(P.field, L.pos, L.dir, L.qop, h, sd);
+      if (err <= P.tol) break;
       const double scale = smin(smax(0.25, pow(P.tol / fabs(2. * err), 0.25)), 4.);
       const double hn = h * scale;
       L.ss[kAccuracy] = hn;

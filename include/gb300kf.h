@@ -132,7 +132,15 @@ typedef struct kf_config {
                                 depend on this field); the batched form runs its
                                 material instantiation (128 threads x 4 CTAs per
                                 SM) whatever the shape fields say */
-  int32_t reserved0;
+  int32_t adjoint_tape;      /* kf_adjoint_batch only: 0 (default) = the forward
+                                records the tape of the whole track (256 doubles
+                                per track and surface, at least 3072); 1 = it
+                                saves checkpoints every 5 measurement states
+                                and the reverse sweep recomputes one 5-state
+                                segment at a time (3072 doubles per track).
+                                The results are bitwise the same; 0 is faster
+                                and is also what a track falls back to 1 from
+                                when its tape runs over */
 } kf_config_t;
 
 /* The surface sequence: boundless plane surfaces (PlaneSurface<InfiniteBounds>,
@@ -339,6 +347,10 @@ typedef struct kf_adjoint_outputs {
   double *grad_field_scale_track; /* [n] d chi2_track / d field scale, or NULL */
 } kf_adjoint_outputs_t;
 
+/* Device workspace bytes kf_adjoint_batch needs: the fit's state store,
+ * the smoother adjoints, checkpoints and the tape, whose size follows
+ * cfg->adjoint_tape (262144 tracks of 20 surfaces: 15.2 GB with 0, 10.9 GB
+ * with 1).  cfg may be NULL (adjoint_tape = 0). */
 size_t kf_adjoint_workspace_size(const kf_config_t *cfg, int64_t n_tracks, int32_t n_surfaces);
 
 /* compute_gradient = 0 runs the forward part only (chi2, status), the

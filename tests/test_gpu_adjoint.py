@@ -176,7 +176,26 @@ def test_gradcheck_through_autograd(kf):
                                     eps=1e-6, atol=1e-3, rtol=1e-4)
 
 
+# adjoint_tape = 0: the forward records the whole track's tape (a track whose
+# tape runs over recomputes from its checkpoints); 1: every track recomputes
+# its 5-state segments from the checkpoints.  Same arithmetic, so every
+# output is bitwise the same.  The second workload (0.5-1 GeV, 10 planes 100
+# mm apart) takes ~70 RK steps a track and runs most tapes over in mode 0.
+@pytest.mark.parametrize("kw", [TEL, dict(n_planes=10, x_first=100., x_step=100., mis_shift=0.1,
+                                          mis_rot=1e-3, p_min=0.5, p_max=1.0)])
+def test_tape_modes_agree_bitwise(kf, kw):
+    tel = kf.make_telescope(3000, seed=99, **kw)
+    r0 = kf.AdjointBatch(tel, kf.default_config(overstep_limit=0.1)).run(grad=True)
+    r1 = kf.AdjointBatch(tel, kf.default_config(overstep_limit=0.1, adjoint_tape=1)).run(grad=True)
+    assert np.mean(r0["status"] == 0) > 0.7
+    for k in r0:
+        assert np.array_equal(r0[k], r1[k]), k
+
+
 def test_adjoint_rejects_unsupported(kf):
     tel = kf.make_telescope(10, seed=1, n_planes=10, field_map=True, field_n=11)
     with pytest.raises(kf.KfError):
         kf.AdjointBatch(tel, kf.default_config()).run(grad=True)
+    tel = kf.make_telescope(10, seed=1, **TEL)
+    with pytest.raises(kf.KfError):
+        kf.AdjointBatch(tel, kf.default_config(adjoint_tape=2)).run(grad=True)
