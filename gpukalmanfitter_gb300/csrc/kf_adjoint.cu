@@ -570,6 +570,10 @@ __device__ double smoothChi2(const Params &P, const AdjParams &A, int64_t u, int
     invJacobian(Jn, G);
     kfa::smoothStep(G, xf, xn, xp, xs);
     for (int e = 0; e < 6; ++e) XS(s, e) = xs[e];
+    // the reverse pass below takes the gain from here: the Jacobian-adjoint
+    // slots of state s + 1 hold it until that pass writes the adjoint there
+    if (grad)
+      for (int e = 0; e < 25; ++e) SB(s + 1, 12 + e) = G[e];
   }
   // chi2 terms and their adjoints d chi2 / d xs = -2 V^-1 r (rows 0, 1)
   double chi2 = 0.;
@@ -594,15 +598,15 @@ __device__ double smoothChi2(const Params &P, const AdjParams &A, int64_t u, int
     return chi2;
   }
   for (int s = 0; s < ns; ++s)
-    for (int e = 0; e < kStateStride; ++e) SB(s, e) = 0.;
+    for (int e = 0; e < (s == 0 ? kStateStride : 12); ++e) SB(s, e) = 0.;
   double xsb[6] = {0., 0., 0., 0., 0., 0.}, g[2];
   term(0, g);
   xsb[0] = g[0];
   xsb[1] = g[1];
   for (int s = 0; s + 1 < ns; ++s) {
-    double Jn[25], G[25], Gb[25], Jb[25], xn[6], xp[6], xfb[6], xnb[6], xpb[6];
+    double G[25], Gb[25], Jb[25], xn[6], xp[6], xfb[6], xnb[6], xpb[6];
     for (int e = 0; e < 25; ++e) {
-      Jn[e] = WS(s + 1, 12 + e);
+      G[e] = SB(s + 1, 12 + e);
       Gb[e] = Jb[e] = 0.;
     }
     for (int e = 0; e < 6; ++e) {
@@ -610,14 +614,13 @@ __device__ double smoothChi2(const Params &P, const AdjParams &A, int64_t u, int
       xp[e] = WS(s + 1, e);
       xfb[e] = xnb[e] = xpb[e] = 0.;
     }
-    invJacobian(Jn, G);
     kfa::smoothStepVjp(G, xn, xp, xsb, xfb, xnb, xpb, Gb);
     kfa::invVjp(G, Gb, Jb);
     for (int e = 0; e < 6; ++e) {
       SB(s, 6 + e) += xfb[e];
       SB(s + 1, e) += xpb[e];
     }
-    for (int e = 0; e < 25; ++e) SB(s + 1, 12 + e) += Jb[e];
+    for (int e = 0; e < 25; ++e) SB(s + 1, 12 + e) = Jb[e];
     term(s + 1, g);
     for (int e = 0; e < 6; ++e) xsb[e] = xnb[e];
     xsb[0] += g[0];

@@ -897,7 +897,8 @@ KF_HD void boundFwd(const BoundIn &in, const Frame &f, BoundOut &o, BoundTmp &w,
   }
   for (int r = 0; r < 6; ++r) J[r][5] = (r == 5) ? 1. : 0.;
   // M = J C and C' = M J^T on the structure: row 4 of J is e4, column 5 is e5
-  for (int i = 0; i < 6; ++i)
+  // (the recomputation needs rows 0-1 only; the VJP does not read M)
+  for (int i = 0; i < (full ? 6 : 2); ++i)
     for (int j = 0; j < 6; ++j) {
       if (i == 4) {
         w.M[4][j] = in.C[si6(4, j)];
@@ -1007,8 +1008,11 @@ KF_HD void boundVjp(const BoundIn &in, const Frame &f, const BoundOut &o, const 
     kb.g46[r][0] = ob.G.g46[r][0];
     kb.g46[r][1] = ob.G.g46[r][1];
   }
-  // ---- C' = J C J^T and the stored Jacobian (J: row 4 = e4, column 5 = e5;
-  // W: the upper-triangle adjoint of C')
+  // ---- C' = J C J^T and the stored Jacobian (J: row 4 = e4, column 5 = e5).
+  // W is the upper-triangle adjoint of C' and Ws = W + W^T; with X = Ws J,
+  //   J-bar = Ws J C = X C on the free entries (rows 0-3, 5; columns 0-4),
+  //   C-bar on the stored triangle = (J^T X)_kl for k < l, (J^T X)_kk / 2
+  // (J^T Ws J is the full-matrix gradient plus its transpose)
   double Ws[6][6], Jb[6][6];
   for (int i = 0; i < 6; ++i)
     for (int j = 0; j < 6; ++j) {
@@ -1016,43 +1020,34 @@ KF_HD void boundVjp(const BoundIn &in, const Frame &f, const BoundOut &o, const 
       Jb[i][j] = 0.;
     }
   const double(&J)[6][6] = w.Jf;
-  // Jb = (W + W^T) J C = (W + W^T) M, on the free entries (rows 0-3,5, cols 0-4)
+  constexpr int kFree[5] = {0, 1, 2, 3, 5}; // J's rows off e4
+  double X[6][6];
   for (int a = 0; a < 6; ++a) {
-    if (a == 4) continue;
+    for (int k = 0; k < 5; ++k) {
+      double s = (k == 4) ? Ws[a][4] : 0.;
+      for (int ii = 0; ii < 5; ++ii) s += Ws[a][kFree[ii]] * J[kFree[ii]][k];
+      X[a][k] = s;
+    }
+    X[a][5] = Ws[a][5];
+  }
+  for (int ai = 0; ai < 5; ++ai) {
+    const int a = kFree[ai];
     for (int b = 0; b < 5; ++b) {
       double s = 0.;
-      for (int i = 0; i < 6; ++i) s += Ws[a][i] * w.M[i][b];
+      for (int k = 0; k < 6; ++k) s += X[a][k] * in.C[si6(k, b)];
       Jb[a][b] += s;
     }
   }
-  // C-bar (full) = J^T (W J), folded onto the stored upper triangle; W is upper
-  // triangular, so row i of W J sums over j >= i
-  double WJ[6][6];
-  for (int i = 0; i < 6; ++i)
-    for (int l = 0; l < 6; ++l) {
-      double t;
-      if (l == 5) {
-        t = ob.Cp[ut6(i, 5)];
-      } else {
-        t = 0.;
-        for (int j = i; j < 6; ++j)
-          if (j != 4) t += ob.Cp[ut6(i, j)] * J[j][l];
-        if (l == 4 && i <= 4) t += ob.Cp[ut6(i, 4)];
-      }
-      WJ[i][l] = t;
-    }
   for (int k = 0; k < 6; ++k)
-    for (int l = 0; l < 6; ++l) {
+    for (int l = k; l < 6; ++l) {
       double s;
       if (k == 5) {
-        s = WJ[5][l];
+        s = X[5][l];
       } else {
-        s = 0.;
-        for (int i = 0; i < 6; ++i)
-          if (i != 4) s += J[i][k] * WJ[i][l];
-        if (k == 4) s += WJ[4][l];
+        s = (k == 4) ? X[4][l] : 0.;
+        for (int ii = 0; ii < 5; ++ii) s += J[kFree[ii]][k] * X[kFree[ii]][l];
       }
-      ib.C[si6(k, l)] += s;
+      ib.C[ut6(k, l)] += (k == l) ? 0.5 * s : s;
     }
   for (int c = 0; c < 5; ++c) {
     Jb[0][c] += ob.Jst[c];
@@ -1368,34 +1363,39 @@ KF_HD void smoothStepVjp(const double Gs[25], const double xsn[6], const double 
     xpnb[e] -= dxb[e];
   }
 }
-// Gb (stored layout, adjoint of G = J^-1) -> Jb (stored layout): Jb = -G^T Gb G^T
+// Gb (stored layout, adjoint of G = J^-1) -> Jb (stored layout): Jb = -G^T Gb G^T,
+// on the structure G and J share (row 4 = e4, column 5 = e5) and Gb's free
+// entries (rows 0-3, 5; columns 0-4): products with the structural zeros and
+// ones are not formed (a product with a literal 0 is not free in IEEE FP64)
 KF_HD void invVjp(const double Gs[25], const double Gb[25], double Jb[25]) {
-  double G[6][6], B[6][6], T[6][6];
-  jstFull(Gs, G);
-  for (int r = 0; r < 6; ++r)
-    for (int c = 0; c < 6; ++c) B[r][c] = 0.;
-  for (int c = 0; c < 5; ++c) {
-    B[0][c] = Gb[c];
-    B[1][c] = Gb[5 + c];
-    B[2][c] = Gb[10 + c];
-    B[3][c] = Gb[15 + c];
-    B[5][c] = Gb[20 + c];
-  }
-  // T = G^T B
-  for (int r = 0; r < 6; ++r)
-    for (int c = 0; c < 6; ++c) {
-      double s = 0.;
-      for (int k = 0; k < 6; ++k) s += G[k][r] * B[k][c];
-      T[r][c] = s;
-    }
-  // Jb = -T G^T, rows 0-3,5 x cols 0-4
-  const int rows[5] = {0, 1, 2, 3, 5};
-  for (int ri = 0; ri < 5; ++ri)
+  // stored row ri of Gs / Gb / Jb is full row kFree[ri]
+  constexpr int kFree[5] = {0, 1, 2, 3, 5};
+  // T = G^T B with B = Gb placed on the free entries: T[r][c] = sum over
+  // free rows k of G[k][r] B[k][c], c < 5 (B's column 5 is 0); row 5 of T is
+  // B's row 5 (G's column 5 is e5)
+  double T[6][5];
+  for (int r = 0; r < 5; ++r)
     for (int c = 0; c < 5; ++c) {
       double s = 0.;
-      for (int k = 0; k < 6; ++k) s += T[rows[ri]][k] * G[c][k];
+      for (int ki = 0; ki < 5; ++ki) s += Gs[5 * ki + r] * Gb[5 * ki + c];
+      T[r][c] = s;
+    }
+  for (int c = 0; c < 5; ++c) T[5][c] = Gb[20 + c];
+  // Jb = -T G^T on the free rows, columns 0-4: sum over k < 5 of T[r][k] G[c][k]
+  // (T's column 5 is 0); G's row 4 is e4, so column 4 takes T[r][4]
+  for (int ri = 0; ri < 5; ++ri) {
+    const int r = kFree[ri];
+    for (int c = 0; c < 5; ++c) {
+      double s;
+      if (c == 4) {
+        s = T[r][4];
+      } else {
+        s = 0.;
+        for (int k = 0; k < 5; ++k) s += T[r][k] * Gs[5 * c + k];
+      }
       Jb[5 * ri + c] -= s;
     }
+  }
 }
 
 // ---------------------------------------------------------------------------
