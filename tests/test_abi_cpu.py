@@ -46,6 +46,31 @@ def test_workspace_size(kf):
     assert lib.kf_host_staging_size(C.byref(cfg), 1000, 10, 0) > 10 * 37 * 1000 * 8
 
 
+def test_adjoint_workspace_and_tape_mode(kf):
+    lib = kf.load()
+    taped = kf.default_config()
+    segments = kf.default_config(adjoint_tape=1)
+    w0 = lib.kf_adjoint_workspace_size(C.byref(taped), 1000, 20)
+    w1 = lib.kf_adjoint_workspace_size(C.byref(segments), 1000, 20)
+    # the whole-track tape holds 256 doubles a surface, the segment mode 3072
+    assert w0 - w1 == (20 * 256 - 3072) * 1000 * 8
+    assert lib.kf_adjoint_workspace_size(None, 1000, 20) == w0
+    assert lib.kf_adjoint_workspace_size(C.byref(taped), 0, 20) == 0
+    # an unknown tape mode is refused before any device work
+    tel = kf.make_telescope(4, n_planes=20, x_first=50., x_step=50.)
+    geo, keep = tel.geometry()
+    fld = tel.field()
+    ins = kf.KfInputs()
+    ins.n_tracks, ins.stride, ins.n_surfaces = 4, 4, 20
+    arr = [np.zeros(8) for _ in range(8)]
+    ins.meas, ins.start_params, ins.start_cov, ins.perigee = (a.ctypes.data for a in arr[:4])
+    outs = kf.KfAdjointOutputs(*(a.ctypes.data for a in arr[4:8]), None, None, None)
+    bad = kf.default_config(adjoint_tape=2)
+    assert lib.kf_adjoint_batch(C.byref(ins), C.byref(outs), C.byref(bad), C.byref(geo),
+                                C.byref(fld), 1, None, 0, None) == -1
+    assert b"adjoint_tape" in lib.kf_last_error_string()
+
+
 def test_argument_validation_without_gpu(kf):
     lib = kf.load()
     cfg = kf.default_config()
