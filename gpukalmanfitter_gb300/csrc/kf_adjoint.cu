@@ -9,17 +9,19 @@
 // warp's lanes take similar numbers of RK steps between surfaces); the
 // adjoint's own workspace is indexed by queue position (coalesced), inputs,
 // outputs and per-track gradient parts by track:
-//   A. forward fit (the fit kernel's own lane program, smoothing off) with a
-//      checkpoint of the whole lane before every 5th measurement state;
+//   A. forward fit (the fit kernel's own lane program, smoothing off) while a
+//      hook records the track's tape (step pre-states and trial step sizes,
+//      step-size constraint updates, surface events), with a checkpoint of
+//      the whole lane before every 5th measurement state;
 //   B. smoother and chi2 from the stored states, then the smoother's reverse
 //      sweep: adjoints of every state's predicted and filtered parameters and
 //      of its bound-to-bound Jacobian;
-//   C. for each 5-state segment, last first: restore the checkpoint, run the
-//      segment again through the same lane program while a hook records a
-//      tape (step pre-states and trial step sizes, step-size constraint
-//      updates, surface events), then sweep the tape backwards with the
-//      vector-Jacobian products of kf_adjoint_math.h.  The last two segments
-//      are taped by the forward itself and are not recomputed.
+//   C. the tape swept backwards with the vector-Jacobian products of
+//      kf_adjoint_math.h.  A track whose tape ran over its capacity (and
+//      every track with kf_config_t.adjoint_tape = 1) instead restores its
+//      checkpoints 5-state segment by segment, last first, runs each segment
+//      again through the same lane program while the hook records it, and
+//      sweeps that.
 // The step size is part of the differentiated function: an accepted step's
 // size carries its adjoint to the constraint that set it (the distance to the
 // next plane, or the accuracy step of an earlier rejected trial, which in
