@@ -78,7 +78,9 @@ __device__ __forceinline__ double hdr(int type, int len) { return (double)(type 
 struct TapeRef {
   const double *p;
   int64_t n;
-  __device__ __forceinline__ double operator[](int k) const { return p[(int64_t)k * n]; }
+  // each word is read once: a streaming load, so that the tape passing
+  // through does not evict the spilled registers and state arrays from L2
+  __device__ __forceinline__ double operator[](int k) const { return __ldcs(p + (int64_t)k * n); }
   __device__ __forceinline__ TapeRef operator+(int k) const { return {p + (int64_t)k * n, n}; }
 };
 
@@ -91,7 +93,7 @@ struct TapeHook {
   bool rec, full, over; // recording; a step failed; the tape ran over its capacity
 
   __device__ __forceinline__ void put(double v) {
-    if (top < cap) tape[(int64_t)top * n] = v;
+    if (top < cap) __stcs(tape + (int64_t)top * n, v); // written once, read once
     else over = true;
     ++top;
   }
@@ -175,15 +177,18 @@ struct TapeHook {
 using ALane = Lane<double, TapeHook>;
 
 // ---- checkpoints: every field of the lane and its cold state --------------
+// checkpoints are read back only by a track whose tape ran over: streaming
+// stores, as for the tape
 struct Saver {
   double *p;
   int64_t n;
   int w;
-  __device__ void operator()(double &x) { p[(int64_t)(w++) * n] = x; }
-  __device__ void operator()(int &x) { p[(int64_t)(w++) * n] = (double)x; }
-  __device__ void operator()(bool &x) { p[(int64_t)(w++) * n] = x ? 1. : 0.; }
-  __device__ void operator()(uint64_t &x) { p[(int64_t)(w++) * n] = __longlong_as_double((long long)x); }
-  __device__ void operator()(int64_t &x) { p[(int64_t)(w++) * n] = __longlong_as_double(x); }
+  __device__ void put(double v) { __stcs(p + (int64_t)(w++) * n, v); }
+  __device__ void operator()(double &x) { put(x); }
+  __device__ void operator()(int &x) { put((double)x); }
+  __device__ void operator()(bool &x) { put(x ? 1. : 0.); }
+  __device__ void operator()(uint64_t &x) { put(__longlong_as_double((long long)x)); }
+  __device__ void operator()(int64_t &x) { put(__longlong_as_double(x)); }
 };
 struct Loader {
   const double *p;
@@ -452,12 +457,13 @@ __device__ void reverseHit(TapeRef w, Adj &R, const Params &P, const PlaneD *sp,
   kfa::BoundOut o, ob;
   kfa::BoundTmp bt;
   kfa::boundFwd(in, f, o, bt, false);
-  // predicted and filtered parameters as the forward stored them
-  auto WS = [&](int e) { return P.ws[((int64_t)s * kStateStride + e) * n + u]; };
+  // predicted parameters as the forward stored them, and below the smoother
+  // adjoints of this state: read once here, long after they were written
+  // (streaming loads)
+  auto WS = [&](int e) { return __ldcs(P.ws + ((int64_t)s * kStateStride + e) * n + u); };
   for (int e = 0; e < 6; ++e) o.pred[e] = WS(e);
-  // smoother adjoints of this state
   const double *sb = A.stateBar + u;
-  auto SB = [&](int e) { return sb[((int64_t)s * kStateStride + e) * n]; };
+  auto SB = [&](int e) { return __ldcs(sb + ((int64_t)s * kStateStride + e) * n); };
   for (int e = 0; e < 6; ++e) ob.pred[e] = SB(e);
   for (int e = 0; e < 25; ++e) ob.Jst[e] = SB(12 + e);
   ob.G = R.G;
