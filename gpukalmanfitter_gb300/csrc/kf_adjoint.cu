@@ -376,7 +376,7 @@ __device__ void reverseStep(TapeRef w, int len, Adj &R, const Params &P, double 
   kfa::polyPrep(dir, B, ps);
   kfa::polyCoef(g.qop, h, ps);
   kfa::PolyOut o;
-  kfa::polyAcceptFwd(pos, dir, t, g.qop, h, g.dtds, g.d37, B, ps, o);
+  kfa::polyAcceptFwd(pos, dir, t, g.qop, h, g.dtds, g.d37, B, ps, o, true);
   // J' = D J
   kfa::DMat Db;
   kfa::dmZero(Db);
@@ -477,12 +477,20 @@ __device__ void reverseHit(TapeRef w, Adj &R, const Params &P, const PlaneD *sp,
     double filt[6], cf[21], chi2;
     kfa::FilterTmp fw;
     kfa::filterFwd(o.pred, o.Cp, mv, filt, cf, &chi2, fw);
+    // the stepper update as the fit does it: the filtered angles' sines and
+    // cosines by angle addition from the predicted direction, the leg
+    // constants from 1/p = |q/p|
     double pos1[3], dir1[3], p1, t1, trig[4];
-    kfa::updateFwd(f, filt, pos1, dir1, &p1, &t1, trig);
+    if (!kfa::trigByAddition(in.dir, filt[2] - o.pred[2], filt[3] - o.pred[3], trig)) {
+      kfa::sinCos(filt[2], trig[0], trig[1]);
+      kfa::sinCos(filt[3], trig[2], trig[3]);
+    }
+    kfa::updateFwdTrig(f, filt, trig, pos1, dir1, &p1, &t1);
     kfa::Leg g;
-    kfa::legFwd(p1, q, P.mass, g);
+    const double ip1 = fabs(filt[4]);
+    kfa::legFwdIp(ip1, q, P.mass, g);
     double pb = R.p;
-    kfa::legVjp(p1, q, P.mass, g, R.qop, R.dtds, R.d37, pb);
+    kfa::legVjpIp(ip1, q, P.mass, g, R.qop, R.dtds, R.d37, pb);
     R.qop = R.dtds = R.d37 = 0.;
     double filtb[6];
     for (int e = 0; e < 6; ++e) filtb[e] = SB(6 + e);

@@ -517,7 +517,7 @@ KF_HD void polyTrialFwd(const double d[3], double q, double h, const double B[3]
 }
 
 struct PolyOut {
-  double pos[3], dir[3], t, k4[3], w[3], n;
+  double pos[3], dir[3], t, k4[3], w[3], n, in; // in = 1 / n
   DMat D;
 };
 // A = the matrix of v -> v x B, A2 = A^2 = B B^T - |B|^2 I
@@ -535,18 +535,31 @@ KF_HD void crossMatrix(const double B[3], double A[3][3], double A2[3][3], doubl
     for (int j = 0; j < 3; ++j) A2[i][j] = B[i] * B[j] - ((i == j) ? beta : 0.);
 }
 
+// fastNorm (the adjoint's reverse sweep, where the step is recomputed only
+// for its derivatives): 1/|w| from rsqrt instead of a square root and a
+// division; the fit's step keeps the latter
 KF_HD void polyAcceptFwd(const double pos[3], const double d[3], double t, double q, double h,
                          double dtds, double d37, const double B[3], const PolyStep &w,
-                         PolyOut &o) {
+                         PolyOut &o, bool fastNorm = false) {
   // constants as products (a division by a literal is a full FP64 division)
   const double h6 = h * (1. / 6.), hh6 = h * h6;
   for (int i = 0; i < 3; ++i) {
     o.pos[i] = pos[i] + (h * d[i] + hh6 * (w.P * w.c[i] + w.Q * w.e[i]));
     o.w[i] = d[i] + h6 * (w.Pd * w.c[i] + w.Qd * w.e[i]);
   }
-  o.n = sqrt(dot(o.w, o.w));
-  const double in = 1. / o.n;
-  for (int i = 0; i < 3; ++i) o.dir[i] = o.w[i] * in;
+  if (fastNorm) {
+    const double n2 = dot(o.w, o.w);
+#ifdef __CUDA_ARCH__
+    o.in = rsqrt(n2);
+#else
+    o.in = 1. / sqrt(n2);
+#endif
+    o.n = n2 * o.in;
+  } else {
+    o.n = sqrt(dot(o.w, o.w));
+    o.in = 1. / o.n;
+  }
+  for (int i = 0; i < 3; ++i) o.dir[i] = o.w[i] * o.in;
   o.t = t + h * dtds;
   const double a4 = q * (1. - 0.5 * w.x), b4 = h * q * q * (1. - 0.25 * w.x);
   for (int i = 0; i < 3; ++i) o.k4[i] = a4 * w.c[i] + b4 * w.e[i];
@@ -697,7 +710,7 @@ KF_HD void polyAcceptVjp(const double d[3], double q, double h, double dtds, dou
     const double pr = dot(o.dir, dirb_);
     double wb[3], wc = 0., we = 0.;
     for (int i = 0; i < 3; ++i) {
-      wb[i] = (dirb_[i] - o.dir[i] * pr) * (1. / o.n);
+      wb[i] = (dirb_[i] - o.dir[i] * pr) * o.in;
       db[i] += wb[i];
       cb[i] += h6 * w.Pd * wb[i];
       eb[i] += h6 * w.Qd * wb[i];
@@ -1202,23 +1215,56 @@ KF_HD void filterVjp(const double C[21], const FilterTmp &w, const double filtb[
 //   pos = c + U x0 + V x1, d = unit(cos x2 sin x3, sin x2 sin x3, cos x3),
 //   p = |1/x4|, t = x5;  qop = q/p, dtds = sqrt(1 + (m/p)^2), d37 = m^2 q/(p dtds)
 // ---------------------------------------------------------------------------
-KF_HD void updateFwd(const Frame &f, const double x[6], double pos[3], double d[3], double *p,
-                     double *t, double trig[4] = nullptr) {
+// the stepper update from the filtered angles' sines and cosines
+// trig = (sin phi, cos phi, sin theta, cos theta)
+KF_HD void updateFwdTrig(const Frame &f, const double x[6], const double trig[4], double pos[3],
+                         double d[3], double *p, double *t) {
   for (int r = 0; r < 3; ++r) pos[r] = f.U[r] * x[0] + f.V[r] * x[1] + f.c[r];
-  double sp, cp, st, ct;
-  sinCos(x[2], sp, cp);
-  sinCos(x[3], st, ct);
-  if (trig) {
-    trig[0] = sp;
-    trig[1] = cp;
-    trig[2] = st;
-    trig[3] = ct;
-  }
+  const double sp = trig[0], cp = trig[1], st = trig[2], ct = trig[3];
   const double v[3] = {cp * st, sp * st, ct};
   const double in = 1. / sqrt(dot(v, v));
   for (int i = 0; i < 3; ++i) d[i] = v[i] * in;
   *p = fabs(1. / x[4]);
   *t = x[5];
+}
+KF_HD void updateFwd(const Frame &f, const double x[6], double pos[3], double d[3], double *p,
+                     double *t, double trig[4] = nullptr) {
+  double tr[4];
+  sinCos(x[2], tr[0], tr[1]);
+  sinCos(x[3], tr[2], tr[3]);
+  if (trig)
+    for (int e = 0; e < 4; ++e) trig[e] = tr[e];
+  updateFwdTrig(f, x, tr, pos, d, p, t);
+}
+// Sines and cosines of the filtered angles phi_p + dphi, theta_p + dth from
+// the predicted unit direction d (cos phi_p = d0 / s, sin phi_p = d1 / s,
+// cos theta_p = d2, sin theta_p = s = |(d0, d1)|) by angle addition, with
+// Taylor series for the corrections (|delta| <= 0.02: truncation below
+// 1e-20), as the fit's stepper update does; false for a larger correction
+// or a direction within 1e-6 of the z axis
+KF_HD bool trigByAddition(const double d[3], double dphi, double dth, double trig[4]) {
+  const double s2 = d[0] * d[0] + d[1] * d[1];
+  if (!(fabs(dphi) <= 0.02) || !(fabs(dth) <= 0.02) || !(s2 > 1e-12)) return false;
+  auto sinCosSmall = [](double x, double &sn, double &cs) {
+    const double x2 = x * x;
+    sn = x + x * x2 * (-1. / 6. + x2 * (1. / 120. + x2 * (-1. / 5040.)));
+    cs = 1. + x2 * (-0.5 + x2 * (1. / 24. + x2 * (-1. / 720. + x2 * (1. / 40320.))));
+  };
+  double sdp, cdp, sdt, cdt;
+  sinCosSmall(dphi, sdp, cdp);
+  sinCosSmall(dth, sdt, cdt);
+#ifdef __CUDA_ARCH__
+  const double is = rsqrt(s2);
+#else
+  const double is = 1. / sqrt(s2);
+#endif
+  const double s = s2 * is;
+  const double cp0 = d[0] * is, sp0 = d[1] * is;
+  trig[0] = sp0 * cdp + cp0 * sdp;
+  trig[1] = cp0 * cdp - sp0 * sdp;
+  trig[2] = s * cdt + d[2] * sdt;
+  trig[3] = d[2] * cdt - s * sdt;
+  return true;
 }
 // sp, cp, st, ct: sin/cos of x[2] and x[3] (as evaluated by updateFwd)
 KF_HD void updateVjp(const Frame &f, const double x[6], const double d[3], const double posb[3],
@@ -1243,11 +1289,10 @@ KF_HD void updateVjp(const Frame &f, const double x[6], const double d[3], const
 }
 
 struct Leg {
-  double qop, dtds, d37;
+  double qop, dtds, d37, idt; // idt = 1 / dtds
 };
-KF_HD void legFwd(double p, double q, double mass, Leg &g) {
-  // the fit's legConstantsIp: one 1/sqrt(1 + (m/p)^2)
-  const double ip = 1. / p;
+// from ip = 1 / p (the fit's legConstantsIp: one 1/sqrt(1 + (m/p)^2))
+KF_HD void legFwdIp(double ip, double q, double mass, Leg &g) {
   g.qop = q * ip;
   const double x = mass * ip, a = 1. + x * x;
 #ifdef __CUDA_ARCH__
@@ -1256,15 +1301,22 @@ KF_HD void legFwd(double p, double q, double mass, Leg &g) {
   const double y = 1. / sqrt(a);
 #endif
   g.dtds = a * y;
+  g.idt = y;
   g.d37 = mass * mass * q * ip * y;
 }
-KF_HD void legVjp(double p, double q, double mass, const Leg &g, double qopb, double dtdsb,
-                  double d37b, double &pb) {
-  const double ip = 1. / p, idt = 1. / g.dtds;
+KF_HD void legFwd(double p, double q, double mass, Leg &g) { legFwdIp(1. / p, q, mass, g); }
+// adjoint of the leg constants w.r.t. p, given ip = 1 / p
+KF_HD void legVjpIp(double ip, double q, double mass, const Leg &g, double qopb, double dtdsb,
+                    double d37b, double &pb) {
+  const double idt = g.idt;
   const double ddt = -(mass * mass) * (ip * ip * ip) * idt;
   pb += qopb * (-q * (ip * ip));
   pb += dtdsb * ddt;
   pb += d37b * (-g.d37 * ip - g.d37 * idt * ddt);
+}
+KF_HD void legVjp(double p, double q, double mass, const Leg &g, double qopb, double dtdsb,
+                  double d37b, double &pb) {
+  legVjpIp(1. / p, q, mass, g, qopb, dtdsb, d37b, pb);
 }
 
 // ---------------------------------------------------------------------------

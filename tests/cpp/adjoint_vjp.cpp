@@ -670,7 +670,8 @@ static double testPolyEquivalence() {
   return worst;
 }
 
-static double testPoly() {
+// fast: the reverse sweep's 1/|w| by rsqrt (polyAcceptFwd's fastNorm)
+static double testPoly(bool fast = false) {
   double worst = 0.;
   for (int t = 0; t < 20; ++t) {
     double d[3];
@@ -679,11 +680,11 @@ static double testPoly() {
     Vec x = {100 * N01(), 10 * N01(), N01(), d[0], d[1], d[2], 3. * U01(),
              (t % 2 ? 1 : -1) * (0.1 + U01()), 5. + 60. * U01(), 1. + 0.01 * U01(), 0.01 * N01(),
              1e-5 * N01(), 1e-5 * N01(), B0[2]};
-    Fn F = [](const Vec &v) {
+    Fn F = [fast](const Vec &v) {
       PolyStep w;
       polyTrialFwd(&v[3], v[7], v[8], &v[11], w);
       PolyOut o;
-      polyAcceptFwd(&v[0], &v[3], v[6], v[7], v[8], v[9], v[10], &v[11], w, o);
+      polyAcceptFwd(&v[0], &v[3], v[6], v[7], v[8], v[9], v[10], &v[11], w, o, fast);
       Vec y(o.pos, o.pos + 3);
       y.insert(y.end(), o.dir, o.dir + 3);
       y.push_back(o.t);
@@ -696,7 +697,7 @@ static double testPoly() {
     PolyStep w;
     polyTrialFwd(&x[3], x[7], x[8], &x[11], w);
     PolyOut o;
-    polyAcceptFwd(&x[0], &x[3], x[6], x[7], x[8], x[9], x[10], &x[11], w, o);
+    polyAcceptFwd(&x[0], &x[3], x[6], x[7], x[8], x[9], x[10], &x[11], w, o, fast);
     DMat Db;
     unpackD(&yb[11], Db);
     Vec xb(14, 0.);
@@ -705,6 +706,25 @@ static double testPoly() {
     polyErrVjp(&x[3], x[7], x[8], &x[11], w, yb[7], &xb[3], xb[7], xb[8], &xb[11]);
     worst = fmax(worst, check(F, x, yb, xb, 1e-5));
   }
+  return worst;
+}
+
+// trigByAddition against sin and cos of the summed angles; a correction
+// above 0.02 rad is refused
+static double testTrigAddition() {
+  double worst = 0.;
+  for (int t = 0; t < 200; ++t) {
+    const double phi = 3. * (2. * U01() - 1.), th = 0.1 + 2.9 * U01();
+    const double d[3] = {cos(phi) * sin(th), sin(phi) * sin(th), cos(th)};
+    const double dphi = 0.02 * (2. * U01() - 1.), dth = 0.02 * (2. * U01() - 1.);
+    double tr[4];
+    if (!trigByAddition(d, dphi, dth, tr)) return 1.;
+    const double ref[4] = {sin(phi + dphi), cos(phi + dphi), sin(th + dth), cos(th + dth)};
+    for (int e = 0; e < 4; ++e) worst = fmax(worst, fabs(tr[e] - ref[e]));
+  }
+  double tr[4];
+  const double d[3] = {1., 0., 0.};
+  if (trigByAddition(d, 0.03, 0., tr) || trigByAddition(d, 0., -0.03, tr)) return 1.;
   return worst;
 }
 
@@ -724,5 +744,7 @@ int main() {
   printf("align %.3e\n", testAlign());
   printf("polyequiv %.3e\n", testPolyEquivalence());
   printf("poly %.3e\n", testPoly());
+  printf("polyfast %.3e\n", testPoly(true));
+  printf("trigadd %.3e\n", testTrigAddition());
   return 0;
 }

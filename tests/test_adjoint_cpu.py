@@ -19,7 +19,7 @@ def vjp_report(tmp_path_factory):
 
 @pytest.mark.parametrize("name", ["stages", "accept", "transport", "jtapply", "path", "scale",
                                   "bound", "filter", "update", "leg", "smooth", "start", "align",
-                                  "polyequiv", "poly"])
+                                  "polyequiv", "poly", "polyfast", "trigadd"])
 def test_vjp_matches_finite_differences(vjp_report, name):
     # worst |analytic - central difference| over the largest gradient component,
     # 20 random points and random output adjoints per primitive
