@@ -22,6 +22,16 @@
 
 namespace kfa {
 
+// 1 / sqrt(a): the device's reciprocal square root (one MUFU seed and Newton
+// steps instead of a square root and a division)
+KF_HD double rsqrtD(double a) {
+#ifdef __CUDA_ARCH__
+  return rsqrt(a);
+#else
+  return 1. / std::sqrt(a);
+#endif
+}
+
 // sine and cosine of one angle (one argument reduction on the device)
 KF_HD void sinCos(double x, double &sn, double &cs) {
 #ifdef __CUDA_ARCH__
@@ -803,8 +813,8 @@ struct DirCoef {
 };
 KF_HD void dirCoefFwd(const double d[3], DirCoef &k) {
   const double x = d[0], y = d[1], z = d[2];
-  const double cosT = z, sinT = sqrt(x * x + y * y);
-  const double invS = 1. / sinT;
+  const double r2 = x * x + y * y, invS = rsqrtD(r2);
+  const double cosT = z, sinT = r2 * invS;
   const double cosP = x * invS, sinP = y * invS;
   k.j24 = -sinP * invS;
   k.j25 = cosP * invS;
@@ -820,9 +830,8 @@ KF_HD void dirCoefFwd(const double d[3], DirCoef &k) {
 }
 KF_HD void dirCoefVjp(const double d[3], const DirCoef &kb, double db[3]) {
   const double x = d[0], y = d[1], z = d[2];
-  // powers of 1/s, s = sqrt(x^2 + y^2), from one reciprocal
-  const double s = sqrt(x * x + y * y), is = 1. / s, ir2 = is * is, is3 = ir2 * is,
-               ir4 = ir2 * ir2;
+  // powers of 1/s, s = sqrt(x^2 + y^2), from one reciprocal square root
+  const double is = rsqrtD(x * x + y * y), ir2 = is * is, is3 = ir2 * is, ir4 = ir2 * ir2;
   // j24 = -y / r2, j25 = x / r2
   db[0] += kb.j24 * (2. * x * y * ir4) + kb.j25 * ((y * y - x * x) * ir4);
   db[1] += kb.j24 * ((y * y - x * x) * ir4) + kb.j25 * (-2. * x * y * ir4);
@@ -999,8 +1008,8 @@ KF_HD void boundVjp(const BoundIn &in, const Frame &f, const BoundOut &o, const 
   }
   {
     const double x = in.dir[0], y = in.dir[1], z = in.dir[2];
-    const double r2 = x * x + y * y, s = sqrt(r2), rho2 = r2 + z * z;
-    const double is = 1. / s, ir2 = is * is, irho2 = 1. / rho2;
+    const double r2 = x * x + y * y, rho2 = r2 + z * z;
+    const double is = rsqrtD(r2), s = r2 * is, ir2 = is * is, irho2 = 1. / rho2;
     // phi = atan2(y, x), theta = atan2(s, z) (scale-free in the momentum)
     ib.dir[0] += ob.pred[2] * (-y * ir2);
     ib.dir[1] += ob.pred[2] * (x * ir2);
@@ -1008,8 +1017,8 @@ KF_HD void boundVjp(const BoundIn &in, const Frame &f, const BoundOut &o, const 
     ib.dir[2] += ob.pred[3] * (-s * irho2);
     ib.dir[0] += sb * x * is;
     ib.dir[1] += sb * y * is;
-    // q/p = q / p
-    ib.p += ob.pred[4] * (-o.pred[4] / in.p);
+    // q/p = q / p: d(q/p)/dp = -q / p^2 = -q (q/p)^2 (q = +-1)
+    ib.p += ob.pred[4] * (-in.q * o.pred[4] * o.pred[4]);
   }
   ib.t += ob.pred[5];
   // ---- new jacToGlobal
@@ -1222,7 +1231,7 @@ KF_HD void updateFwdTrig(const Frame &f, const double x[6], const double trig[4]
   for (int r = 0; r < 3; ++r) pos[r] = f.U[r] * x[0] + f.V[r] * x[1] + f.c[r];
   const double sp = trig[0], cp = trig[1], st = trig[2], ct = trig[3];
   const double v[3] = {cp * st, sp * st, ct};
-  const double in = 1. / sqrt(dot(v, v));
+  const double in = rsqrtD(dot(v, v));
   for (int i = 0; i < 3; ++i) d[i] = v[i] * in;
   *p = fabs(1. / x[4]);
   *t = x[5];
@@ -1278,7 +1287,7 @@ KF_HD void updateVjp(const Frame &f, const double x[6], const double d[3], const
     fb.c[r] += posb[r];
   }
   const double v[3] = {cp * st, sp * st, ct};
-  const double in = 1. / sqrt(dot(v, v));
+  const double in = rsqrtD(dot(v, v));
   const double pr = dot(d, db);
   double vb[3];
   for (int i = 0; i < 3; ++i) vb[i] = (db[i] - d[i] * pr) * in;
