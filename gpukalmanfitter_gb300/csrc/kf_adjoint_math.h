@@ -559,11 +559,7 @@ KF_HD void polyAcceptFwd(const double pos[3], const double d[3], double t, doubl
   }
   if (fastNorm) {
     const double n2 = dot(o.w, o.w);
-#ifdef __CUDA_ARCH__
-    o.in = rsqrt(n2);
-#else
-    o.in = 1. / sqrt(n2);
-#endif
+    o.in = rsqrtD(n2);
     o.n = n2 * o.in;
   } else {
     o.n = sqrt(dot(o.w, o.w));
@@ -1262,12 +1258,7 @@ KF_HD bool trigByAddition(const double d[3], double dphi, double dth, double tri
   double sdp, cdp, sdt, cdt;
   sinCosSmall(dphi, sdp, cdp);
   sinCosSmall(dth, sdt, cdt);
-#ifdef __CUDA_ARCH__
-  const double is = rsqrt(s2);
-#else
-  const double is = 1. / sqrt(s2);
-#endif
-  const double s = s2 * is;
+  const double is = rsqrtD(s2), s = s2 * is;
   const double cp0 = d[0] * is, sp0 = d[1] * is;
   trig[0] = sp0 * cdp + cp0 * sdp;
   trig[1] = cp0 * cdp - sp0 * sdp;
